@@ -1,0 +1,330 @@
+#!/usr/bin/env python
+"""Throughput of the fused Bloch–Torrey step on GB300: voxel-steps/s and the
+fraction of the HBM roofline it reaches.
+
+Workload (one GPU): 256^3 sphere pack (radius 10 voxels, solid fraction 0.4),
+face velocities from the curl of Gaussian-smoothed (sigma 4) vector noise,
+zero on solid faces, max |v| = 1 mm/s, PGSE along z (G = 0.1 T/m, delta = 2 ms,
+Delta = 20 ms, gamma = 2.675e8 rad/s/T) with a 180 degree refocusing pulse,
+complex Mxy + Mz in FP32 (k-space exact-precession scheme), dx = 1 um,
+D = 2.3e-9 m^2/s, T1 = 2.5 s, T2 = 2.0 s, rho = 10 um/s, dt = 0.9 dx^2/(6D).
+Seeded synthetic inputs stand in for the reference's missing Poro/Vx/Vy/Vz.
+
+One bench step = STEPS_PER_ITER (100) time steps of the whole field (one
+M(t) sample per time step). Every time step streams ~620 MB through HBM, so
+the working set exceeds the 129 MB L2 between timed iterations.
+
+--impl reference times the reference's CPU update (the oracle port of
+ExplicitSimple, FP64, all host threads) on a bounded sample of the same
+workload. Multi-GPU runs are replicas (one independent field per GPU, no
+data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "voxel-steps/s/GB300 (%HBM roofline)"
+UNIT = "voxel-steps/s"
+SHAPE = (256, 256, 256)
+STEPS_PER_ITER = 100
+BYTES_PER_VOXEL_STEP = 37  # FP32: state read 12 + write 12 + face velocities 12 + geometry code 1
+SEED = 20261203
+WORKLOAD = "C2: 256^3 sphere pack r=10 phi_s=0.4, curl-noise flow 1 mm/s, PGSE z G=0.1 T/m d=2 ms D=20 ms, FP32 Mxy+Mz"
+
+
+def rank_info():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return r, w, lr
+
+
+def build_workload(device="cpu", seed=SEED):
+    from initializator_gb300 import geometry
+    mask = geometry.sphere_pack(SHAPE, 10.0, 0.4, seed=seed, device=device)
+    vel = geometry.curl_velocity(mask, 4.0, 1.0e-3, seed=seed + 1, device=device)
+    return mask, vel
+
+
+def physics(total_steps):
+    import initializator_gb300 as bt
+    from initializator_gb300 import geometry
+    dt = geometry.stable_dt(1e-6, 2.3e-9)
+    wave = bt.kspace_waveform_pgse(total_steps, dt, 0.1, 2e-3, 20e-3, axis=(0.0, 0.0, 1.0))
+    rf = [(bt.pgse_refocus_step(dt, 20e-3), 2, math.pi, (1.0, 0.0, 0.0))]
+    kw = dict(dx=1e-6, dt=dt, d_pore=2.3e-9, t1=2.5, t2=2.0, rho1=1e-5, rho2=1e-5, p_eq=1.0, velocity=1,
+              diffusion=1, gamma=bt.GAMMA_PROTON)
+    return kw, wave, rf
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "step_kernel_kspace_256.md")
+    try:
+        with open(p) as f:
+            m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def cpu_baseline(mask, vel, seconds=6.0):
+    """The oracle (FP64 restatement of the reference's ExplicitSimple) on all
+    host cores over a bounded sample of the workload."""
+    import oracle
+    kw, wave, _ = physics(64)
+    threads = os.cpu_count() or 1
+    p = oracle.make_params(SHAPE, dx=kw["dx"], dt=kw["dt"], main_field=(0.0, 0.0, 1.0), gamma=kw["gamma"],
+                           d_pore=kw["d_pore"], t1=kw["t1"], t2=kw["t2"], rho1=kw["rho1"], rho2=kw["rho2"],
+                           p_eq=1.0, vector_mult=1, velocity=1, diffusion=1)
+    st0 = np.zeros((3,) + SHAPE)
+    st0[0] = mask
+    oracle.run(p, mask, st0, 1, vel=vel, grad_wave=wave[:1], threads=threads)
+    one = oracle.last_loop_seconds()
+    n = max(1, min(int(seconds / max(one, 1e-3)), 50))
+    oracle.run(p, mask, st0, n, vel=vel, grad_wave=wave[:n], threads=threads)
+    el = oracle.last_loop_seconds()
+    nvox = int(np.prod(SHAPE))
+    return {"value": nvox * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} time steps of the 256^3 workload, FP64, reference update (Euler cross product, "
+                      f"PGSE waveform), OpenMP over z-planes, {el:.1f} s"}
+
+
+def run_reference(args):
+    r, w, _ = rank_info()
+    if r != 0:
+        return
+    mask, vel = build_workload("cpu")
+    import oracle
+    oracle.build()
+    kw, wave, _ = physics(4096)
+    threads = os.cpu_count() or 1
+    p = oracle.make_params(SHAPE, dx=kw["dx"], dt=kw["dt"], main_field=(0.0, 0.0, 1.0), gamma=kw["gamma"],
+                           d_pore=kw["d_pore"], t1=kw["t1"], t2=kw["t2"], rho1=kw["rho1"], rho2=kw["rho2"],
+                           p_eq=1.0, vector_mult=1, velocity=1, diffusion=1)
+    st = np.zeros((3,) + SHAPE)
+    st[0] = mask
+    per = 1  # time steps per bench step: a bounded sample keeps the run to minutes
+    for i in range(args.warmup):
+        st, _ = oracle.run(p, mask, st, per, vel=vel, grad_wave=wave[i * per:(i + 1) * per], threads=threads)
+    el = 0.0  # stepping-loop time only (the oracle's per-call array set-up is not the reference's cost)
+    for i in range(args.steps):
+        j = args.warmup + i
+        st, _ = oracle.run(p, mask, st, per, vel=vel, grad_wave=wave[j * per:(j + 1) * per], threads=threads)
+        el += oracle.last_loop_seconds()
+    nvox = int(np.prod(SHAPE))
+    v = nvox * per * args.steps / el
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": list(SHAPE), "steps_per_iter": per,
+                   "note": "reference CPU update via the oracle port (the reference sources are not on the GPU box)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{per} time step per bench step of the 256^3 workload, FP64, all host threads"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+
+    import initializator_gb300 as bt
+    from initializator_gb300 import build as bt_build
+    r, w, lr = rank_info()
+    torch.cuda.set_device(lr)
+    if w > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    bt_build.build()
+    S = STEPS_PER_ITER
+    total = (args.warmup + args.steps) * S + (args.steps + 1) * S + 16
+    mask, vel = build_workload(f"cuda:{lr}", seed=SEED + r)
+    kw, wave, rf = physics(total)
+    nvox = int(np.prod(SHAPE))
+    s = bt.Solver(bt.make_config(SHAPE, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, **kw))
+    s.upload_geometry(mask, vel)
+    s.set_schedule(rf, grad_wave=wave)
+    st0 = np.zeros((3,) + SHAPE)
+    st0[0] = mask
+    s.set_state(st0)
+    stream = torch.cuda.ExternalStream(s.stream_ptr)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if w > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- device-resident throughput (value) ----
+    for _ in range(args.warmup):
+        s.run_async(S)
+    s.synchronize()
+    barrier()
+    clocks = ClockSampler(lr)
+    clocks.start()
+    l0 = s.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        s.run_async(S)
+    ev1.record(stream)
+    s.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = s.launches - l0
+    ms = ev0.elapsed_time(ev1)
+    mt = s.read_mt(S)
+    if not np.all(np.isfinite(mt)):
+        raise RuntimeError("non-finite M(t)")
+    if w > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = nvox * S * args.steps * w / (ms / 1e3)
+    per_launch_s = ms / 1e3 / (args.steps * S)
+    achieved = BYTES_PER_VOXEL_STEP * nvox / per_launch_s / 1e9
+    peak, peak_kind = hbm_peak()
+
+    # ---- end to end through the C ABI with host buffers (e2e) ----
+    host_state = np.ascontiguousarray(st0)
+    s.set_step(0)
+    s.set_state(host_state)
+    s.run(S)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.set_state(host_state)  # H2D of the step's input field
+        s.run(S)                 # S time steps, D2H of the S M(t) samples
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if w > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = nvox * S * args.steps * w / e2e_s
+    s.close()
+
+    out = None
+    if r == 0:
+        cpu = None if args.no_cpu_baseline else cpu_baseline(mask, vel)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": w, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": list(SHAPE), "steps_per_iter": S, "seed": SEED,
+                       "scheme": "kspace (exact precession), FP64 M(t) and phase",
+                       "l2": "inputs larger than L2 (~620 MB streamed per time step)",
+                       "parallelism": f"replicas x{w}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "bytes_per_voxel_step": BYTES_PER_VOXEL_STEP, "traffic": profiled_traffic()},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * 4 * nvox,
+                    "d2h_bytes_per_step": 3 * 8 * S},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(out))
+    if w > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,167 @@
+/*
+ * bt.h — C ABI of the GB300 (sm_103a) Bloch–Torrey magnetization solver.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes. Host
+ * buffers belong to the caller, device memory to the library; no pointer
+ * escapes. A handle is used by one host thread at a time and owns one CUDA
+ * stream; several handles may share a device.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the reference project soleh00/Initializator).
+ *
+ * Array layouts (x fastest, 0-based interior cells, no ghost layer):
+ *   mask  [nz][ny][nx]     uint8, 1 = pore (actCell '1'), 0 = solid
+ *   field [nz][ny][nx]     double, one array per component
+ *   vx    [nz][ny][nx+1]   face velocities (already times VEL_MULT); face i is
+ *   vy    [nz][ny+1][nx]   the low face of cell i, face nx the high face of
+ *   vz    [nz+1][ny][nx]   the last cell (Vx/Vy/Vz.dat, cpp:1435-1536)
+ */
+#ifndef BT_H
+#define BT_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference prints and calls exit(), headers/NmrRelaxationSolve.h:14-27) */
+#define BT_OK 0
+#define BT_E_ARG (-1)      /* bad argument or size */
+#define BT_E_CUDA (-2)     /* CUDA runtime error; see bt_last_error */
+#define BT_E_NAN (-3)      /* M(t) watchdog: a sum became NaN/Inf */
+#define BT_E_STATE (-4)    /* call out of order (e.g. run before geometry) */
+#define BT_E_NOMEM (-5)    /* device allocation failed */
+#define BT_E_TIMEOUT (-6)  /* a bounded device wait gave up */
+
+/* precision of the fields and of the per-step arithmetic */
+#define BT_F32 0
+#define BT_F64 1
+
+/* BT_SCHEME_REFERENCE: the reference's explicit upwind update
+ *   (ExplicitSimple, src/NmrRelaxationSolve.cpp:3148-3282): forward Euler
+ *   relaxation toward p_eq*n, Euler cross product M x B_noise with
+ *   B_noise = (Gx*x, Gy*y, Gz*z), first-order upwind advection on face
+ *   velocities, harmonic-mean diffusion; solid voxels stay zero.
+ * BT_SCHEME_KSPACE: physics form, B0 along z. The same relaxation,
+ *   advection and diffusion stencil, but the gradient precession
+ *   exp(-i*gamma*(G.r)*dt) is exact: the transverse field is carried in the
+ *   frame of the wave vector k(t) = gamma * int G dt, accumulated in FP64 on
+ *   the host, and enters the stencil as per-step face phase factors.
+ *   Fields passed in and out are always in the lab frame. */
+#define BT_SCHEME_REFERENCE 0
+#define BT_SCHEME_KSPACE 1
+
+typedef struct bt_config {
+    int nx, ny, nz;        /* interior cells (Nmr_start.dat: ik, jk, kk) */
+    int precision;         /* BT_F32 / BT_F64 */
+    int scheme;            /* BT_SCHEME_* */
+    int vector_mult;       /* NVECTOR: 1 = precession on (REFERENCE scheme) */
+    int velocity;          /* NVELOC: 1 = advection on */
+    int diffusion;         /* NDIFFUS: 1 = diffusion on */
+    int buffer[3];         /* bufferX/Y/Z: cells trimmed from each side of the M(t) sums */
+    int reserved;
+    double dx, dy, dz;     /* voxel edges, m */
+    double dt;             /* time step, s */
+    double main_field[3];  /* mainField vector (FillInMainField, cpp:1944-1962); its unit vector is n */
+    double gamma;          /* gyromagnetic constant g (the reference hard-codes 4.78941714e7) */
+    double grad[3];        /* static gradient GRAD_X/Y/Z, T/m (used when no waveform is set) */
+    double d_pore;         /* diffusivity of a pore voxel, m^2/s */
+    double t1, t2;         /* bulk relaxation times of the fluid, s */
+    double rho1, rho2;     /* surface relaxivities, m/s (rate rho/d per solid face) */
+    double p_eq;           /* equilibriumMagnetization (cpp:810) */
+} bt_config;
+
+/* An instantaneous pulse applied right after the update of step `step`
+ * (AddImpulse flag/param/axis, cpp:2552-2608): flag 1 linear-gradient phase
+ * param*g*(x*dx*ax + y*dy*ay + z*dz*az) about the normalised axis; flag 2 RF
+ * rotation by param about axis; flags 3 and 4 as the reference. The
+ * KSPACE scheme accepts flag 2 only (gradients come from the waveform). */
+typedef struct bt_pulse {
+    long long step;
+    int flag;
+    int reserved;
+    double param;
+    double axis[3];
+} bt_pulse;
+
+typedef struct bt_handle bt_handle;
+
+/* Allocate a solver on the current CUDA device (replaces InitializeGpu,
+ * src/NmrRelaxationSolveKernels.cu:12-88: 27 cudaMalloc of ghosted FP64 grids). */
+int bt_create(const bt_config* cfg, bt_handle** out);
+int bt_destroy(bt_handle* h);
+/* Message of the last failure on this handle ("" when none). */
+const char* bt_last_error(const bt_handle* h);
+
+/* Geometry and flow from host buffers (replaces ReadActiveCells +
+ * FillInDiffusinAndTime + ReadVelocity + the H2D copies of InitializeGpu,
+ * cpp:819-878, 1435-1536, 1756-1893). vx/vy/vz may be NULL when velocity == 0. */
+int bt_upload_geometry(bt_handle* h, const uint8_t* mask,
+                       const double* vx, const double* vy, const double* vz);
+
+/* Whole field in / out in the lab frame (replaces FillInMagnetization,
+ * cpp:2472-2517, and the D2H copies of solve_gpu, cu:1193-1201). */
+int bt_set_state(bt_handle* h, const double* mx, const double* my, const double* mz);
+int bt_get_state(bt_handle* h, double* mx, double* my, double* mz);
+/* The same through device pointers of the handle's precision (float or
+ * double, same layout), for callers whose data is already in HBM. */
+int bt_set_state_device(bt_handle* h, const void* mx, const void* my, const void* mz);
+
+/* Pulse list and per-step gradient waveform (replaces Sequence_gpu,
+ * cpp:2681-3146, which rotates the whole field on the host). grad_wave holds
+ * 3*nwave doubles (T/m) for steps [0, nwave); NULL keeps cfg->grad. */
+int bt_set_schedule(bt_handle* h, const bt_pulse* pulses, int npulses,
+                    const double* grad_wave, long long nwave);
+
+/* Current step index (0 after bt_create); bt_set_step rewinds or advances the
+ * schedule position without touching the field. */
+long long bt_step_index(const bt_handle* h);
+int bt_set_step(bt_handle* h, long long step);
+
+/* Advance nsteps steps (replaces the solve_gpu time loop, cu:1187-1288, with
+ * ExplicitMakUpgrade + Sequence_gpu + BoundaryConditionsForVectorField_gpu +
+ * OutputX/Y/Z). mt_out (host, may be NULL) receives 3*nsteps doubles: the
+ * M(t) sums (x, y, z) after each step and its pulses. Synchronous. */
+int bt_run(bt_handle* h, long long nsteps, double* mt_out);
+
+/* Asynchronous form for timing and pipelines: M(t) stays in the handle's
+ * device buffer; bt_read_mt copies the sums of the last bt_run_async. */
+int bt_run_async(bt_handle* h, long long nsteps);
+int bt_read_mt(bt_handle* h, double* mt_out, long long nsteps);
+int bt_synchronize(bt_handle* h);
+/* The handle's stream as a cudaStream_t (void* keeps this header CUDA-free). */
+void* bt_stream(bt_handle* h);
+
+/* M(t) sums of the current field (OutputX/Y/Z, cpp:3301-3461). */
+int bt_measure(bt_handle* h, double* sums3);
+
+/* Number of kernel launches this handle has issued (a launch inside a replayed
+ * CUDA graph counts once per replay). */
+long long bt_launch_count(const bt_handle* h);
+
+/* ---- host-only helpers (no GPU needed) ---- */
+
+/* Parameters of the reference's pulse schedules. */
+typedef struct bt_sequence_params {
+    int n_sequence;          /* NSEQUENCE: 0 FID, 1 CPMG, 2 PFG, 5 inversion, 9, 98, 99 */
+    int gpu_variant;         /* 1: Sequence_gpu (cpp:2681-3146), 0: Sequence (cpp:2610-2679) */
+    double dt;               /* dTime */
+    double time1, time2;     /* TIME1, TIME2 */
+    double direction[3];     /* field direction (ReadStart, cpp:783-795) */
+    double gradient_pulse;   /* gradientPulse (Nmr_grad.dat line PulseNum[0]) */
+    double multiple_gradients[3];  /* multipleGradients (lines PulseNum[0..2]) */
+} bt_sequence_params;
+
+/* Replay the reference's schedule over steps [0, nsteps) and list the pulses
+ * it applies (time windows [t, t+dt) at currentTime = i*dt, one-shot flags as
+ * the reference). Writes at most cap pulses; *count gets the total. */
+int bt_sequence_schedule(const bt_sequence_params* sp, long long nsteps,
+                         bt_pulse* out, int cap, int* count);
+
+/* Library version string. */
+const char* bt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BT_H */

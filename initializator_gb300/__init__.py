@@ -1,0 +1,278 @@
+"""GB300-native Bloch–Torrey magnetization solver (drop-in for the reference's
+``NmrRelaxationSolve`` stepper).
+
+The compute path is ``_build/libbt.so`` (hand-written sm_103a CUDA behind the
+C ABI of ``include/bt.h``); this module is a thin ctypes binding of that ABI
+for tests, benchmarks and Python callers. There is no CPU fallback: when the
+library is missing, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libbt.so")
+
+BT_OK = 0
+BT_F32, BT_F64 = 0, 1
+BT_SCHEME_REFERENCE, BT_SCHEME_KSPACE = 0, 1
+GAMMA_REFERENCE = 4.78941714e7   # the reference's hard-coded g (cpp:807)
+GAMMA_PROTON = 2.675e8            # rad/s/T
+
+
+class BtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"bt error {code}: {msg}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    """bt_config of include/bt.h."""
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("precision", ctypes.c_int), ("scheme", ctypes.c_int),
+        ("vector_mult", ctypes.c_int), ("velocity", ctypes.c_int), ("diffusion", ctypes.c_int),
+        ("buffer", ctypes.c_int * 3), ("reserved", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
+        ("main_field", ctypes.c_double * 3), ("gamma", ctypes.c_double), ("grad", ctypes.c_double * 3),
+        ("d_pore", ctypes.c_double), ("t1", ctypes.c_double), ("t2", ctypes.c_double),
+        ("rho1", ctypes.c_double), ("rho2", ctypes.c_double), ("p_eq", ctypes.c_double),
+    ]
+
+
+class Pulse(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_longlong), ("flag", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("param", ctypes.c_double), ("axis", ctypes.c_double * 3)]
+
+
+class SequenceParams(ctypes.Structure):
+    _fields_ = [("n_sequence", ctypes.c_int), ("gpu_variant", ctypes.c_int), ("dt", ctypes.c_double),
+                ("time1", ctypes.c_double), ("time2", ctypes.c_double), ("direction", ctypes.c_double * 3),
+                ("gradient_pulse", ctypes.c_double), ("multiple_gradients", ctypes.c_double * 3)]
+
+
+# every symbol include/bt.h declares
+EXPORTS = [
+    "bt_create", "bt_destroy", "bt_last_error", "bt_upload_geometry", "bt_set_state", "bt_get_state",
+    "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
+    "bt_read_mt", "bt_synchronize", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
+    "bt_version",
+]
+
+_lib = None
+
+
+def lib():
+    """Load libbt.so (build it first with initializator_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run `python -m initializator_gb300.build` "
+                           "(the solver has no CPU fallback)")
+    l = ctypes.CDLL(LIB_PATH)
+    vp, dp, ll, i = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_longlong, ctypes.c_int
+    sig = {
+        "bt_create": ([ctypes.POINTER(Config), ctypes.POINTER(vp)], i),
+        "bt_destroy": ([vp], i),
+        "bt_last_error": ([vp], ctypes.c_char_p),
+        "bt_upload_geometry": ([vp, vp, dp, dp, dp], i),
+        "bt_set_state": ([vp, dp, dp, dp], i),
+        "bt_get_state": ([vp, dp, dp, dp], i),
+        "bt_set_state_device": ([vp, vp, vp, vp], i),
+        "bt_set_schedule": ([vp, ctypes.POINTER(Pulse), i, dp, ll], i),
+        "bt_step_index": ([vp], ll),
+        "bt_set_step": ([vp, ll], i),
+        "bt_run": ([vp, ll, dp], i),
+        "bt_run_async": ([vp, ll], i),
+        "bt_read_mt": ([vp, dp, ll], i),
+        "bt_synchronize": ([vp], i),
+        "bt_stream": ([vp], vp),
+        "bt_measure": ([vp, dp], i),
+        "bt_launch_count": ([vp], ll),
+        "bt_sequence_schedule": ([ctypes.POINTER(SequenceParams), ll, ctypes.POINTER(Pulse), i,
+                                  ctypes.POINTER(ctypes.c_int)], i),
+        "bt_version": ([], ctypes.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(l, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = l
+    return l
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_config(shape, *, dx, dy=None, dz=None, dt, precision=BT_F32, scheme=BT_SCHEME_REFERENCE,
+                main_field=(1.0, 0.0, 0.0), gamma=GAMMA_REFERENCE, grad=(0.0, 0.0, 0.0), d_pore=2.3e-9,
+                t1=2.5, t2=2.0, rho1=0.0, rho2=0.0, p_eq=1.0, vector_mult=0, velocity=0, diffusion=1,
+                buffer=(0, 0, 0)) -> Config:
+    nz, ny, nx = shape
+    c = Config()
+    c.nx, c.ny, c.nz = nx, ny, nz
+    c.precision, c.scheme = precision, scheme
+    c.vector_mult, c.velocity, c.diffusion = vector_mult, velocity, diffusion
+    c.buffer[:] = list(buffer)
+    c.dx = dx
+    c.dy = dx if dy is None else dy
+    c.dz = dx if dz is None else dz
+    c.dt = dt
+    c.main_field[:] = list(main_field)
+    c.gamma = gamma
+    c.grad[:] = list(grad)
+    c.d_pore, c.t1, c.t2, c.rho1, c.rho2, c.p_eq = d_pore, t1, t2, rho1, rho2, p_eq
+    return c
+
+
+def sequence_schedule(n_sequence, nsteps, *, dt, time1=0.0, time2=0.0, direction=(1.0, 0.0, 0.0),
+                      gradient_pulse=0.0, multiple_gradients=(0.0, 0.0, 0.0), gpu_variant=True):
+    """The reference's pulse schedule as a list of (step, flag, param, axis) (host only)."""
+    sp = SequenceParams()
+    sp.n_sequence, sp.gpu_variant, sp.dt, sp.time1, sp.time2 = n_sequence, int(gpu_variant), dt, time1, time2
+    sp.direction[:] = list(direction)
+    sp.gradient_pulse = gradient_pulse
+    sp.multiple_gradients[:] = list(multiple_gradients)
+    count = ctypes.c_int(0)
+    rc = lib().bt_sequence_schedule(ctypes.byref(sp), nsteps, None, 0, ctypes.byref(count))
+    if rc:
+        raise BtError(rc, "bt_sequence_schedule")
+    arr = (Pulse * max(1, count.value))()
+    lib().bt_sequence_schedule(ctypes.byref(sp), nsteps, arr, count.value, ctypes.byref(count))
+    return [(int(p.step), int(p.flag), float(p.param), tuple(p.axis)) for p in arr[: count.value]]
+
+
+class Solver:
+    """One bt_handle: the field, its geometry and its schedule on the current GPU."""
+
+    def __init__(self, cfg: Config):
+        self._l = lib()
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        rc = self._l.bt_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc:
+            raise BtError(rc, "bt_create failed")
+        self._h = h
+        self.shape = (cfg.nz, cfg.ny, cfg.nx)
+
+    def _check(self, rc, what):
+        if rc:
+            raise BtError(rc, f"{what}: {self._l.bt_last_error(self._h).decode()}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._l.bt_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload_geometry(self, mask, vel=None):
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        assert mask.shape == self.shape
+        if vel is None:
+            self._check(self._l.bt_upload_geometry(self._h, mask.ctypes.data, None, None, None), "upload_geometry")
+        else:
+            vx, vy, vz = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+            nz, ny, nx = self.shape
+            assert vx.shape == (nz, ny, nx + 1) and vy.shape == (nz, ny + 1, nx) and vz.shape == (nz + 1, ny, nx)
+            self._check(self._l.bt_upload_geometry(self._h, mask.ctypes.data, _dp(vx), _dp(vy), _dp(vz)),
+                        "upload_geometry")
+
+    def set_state(self, state):
+        st = [np.ascontiguousarray(state[c], dtype=np.float64) for c in range(3)]
+        self._check(self._l.bt_set_state(self._h, _dp(st[0]), _dp(st[1]), _dp(st[2])), "set_state")
+
+    def set_state_device(self, tensors):
+        """tensors: three contiguous CUDA tensors of the handle's precision."""
+        self._check(self._l.bt_set_state_device(self._h, *(ctypes.c_void_p(t.data_ptr()) for t in tensors)),
+                    "set_state_device")
+
+    def get_state(self):
+        out = np.zeros((3,) + self.shape)
+        self._check(self._l.bt_get_state(self._h, _dp(out[0]), _dp(out[1]), _dp(out[2])), "get_state")
+        return out
+
+    def set_schedule(self, pulses=(), grad_wave=None):
+        arr = (Pulse * max(1, len(pulses)))()
+        for n, (step, flag, param, axis) in enumerate(pulses):
+            arr[n].step, arr[n].flag, arr[n].param = int(step), int(flag), float(param)
+            arr[n].axis[:] = [float(a) for a in axis]
+        gw = None
+        nwave = 0
+        if grad_wave is not None:
+            gw = np.ascontiguousarray(grad_wave, dtype=np.float64).reshape(-1, 3)
+            nwave = gw.shape[0]
+        self._check(self._l.bt_set_schedule(self._h, arr, len(pulses), _dp(gw), nwave), "set_schedule")
+
+    @property
+    def step(self):
+        return int(self._l.bt_step_index(self._h))
+
+    def set_step(self, step):
+        self._check(self._l.bt_set_step(self._h, int(step)), "set_step")
+
+    def run(self, nsteps):
+        mt = np.zeros((max(1, nsteps), 3))
+        self._check(self._l.bt_run(self._h, int(nsteps), _dp(mt)), "run")
+        return mt[:nsteps]
+
+    def run_async(self, nsteps):
+        self._check(self._l.bt_run_async(self._h, int(nsteps)), "run_async")
+
+    def read_mt(self, nsteps):
+        mt = np.zeros((max(1, nsteps), 3))
+        self._check(self._l.bt_read_mt(self._h, _dp(mt), int(nsteps)), "read_mt")
+        return mt[:nsteps]
+
+    def synchronize(self):
+        self._check(self._l.bt_synchronize(self._h), "synchronize")
+
+    @property
+    def stream_ptr(self):
+        return self._l.bt_stream(self._h)
+
+    def measure(self):
+        out = np.zeros(3)
+        self._check(self._l.bt_measure(self._h, _dp(out)), "measure")
+        return out
+
+    @property
+    def launches(self):
+        return int(self._l.bt_launch_count(self._h))
+
+
+def kspace_waveform_pgse(nsteps, dt, g_amp, delta, Delta, axis=(0.0, 0.0, 1.0)):
+    """Per-step gradient (T/m) of a PGSE sequence: lobes of length delta at
+    [0, delta) and [Delta, Delta + delta), both positive (a 180 pulse at Delta/2
+    between them refocuses). Step i covers [i*dt, (i+1)*dt); its value is the
+    lobe's fraction of that interval."""
+    t0 = np.arange(nsteps) * dt
+    t1 = t0 + dt
+
+    def overlap(a, b):
+        return np.clip(np.minimum(t1, b) - np.maximum(t0, a), 0.0, None) / dt
+
+    f = overlap(0.0, delta) + overlap(Delta, Delta + delta)
+    ax = np.asarray(axis, dtype=np.float64)
+    return (f[:, None] * g_amp) * ax[None, :]
+
+
+def pgse_refocus_step(dt, Delta):
+    """Step after whose update the 180-degree pulse of a PGSE sequence is applied."""
+    return max(0, int(math.ceil(Delta / 2.0 / dt)) - 1)

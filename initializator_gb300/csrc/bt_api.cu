@@ -1,0 +1,629 @@
+// Host runtime behind include/bt.h: handles, device memory, the per-step
+// schedule table and the CUDA-graph-replayed step loop.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bt.h"
+#include "bt_internal.h"
+
+namespace {
+
+constexpr double SMALL = 1.0e-50;
+constexpr int GRAPH_STEPS = 32;   // steps per captured graph (even: state returns to the same buffer)
+constexpr int SUMS_BLOCKS = 1216; // 152 SMs x 8
+
+struct Dev {
+    void* p = nullptr;
+    size_t n = 0;
+};
+
+}  // namespace
+
+struct bt_handle {
+    bt_config cfg{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    size_t esz = 4;               // element size of the fields
+    size_t nvox = 0;
+    void* state[2][3] = {};
+    int cur = 0;
+    uint8_t* code = nullptr;
+    void* vel[3] = {};
+    bt::StepInfo* steps_d = nullptr;
+    long long nsched = 0;
+    std::vector<bt::StepInfo> steps_h;
+    std::vector<double> kpos;     // wave vector at the start of each step (KSPACE), 3 per step
+    bt::DevPulse* pulses_d = nullptr;
+    bt::Ctl* ctl_d = nullptr;
+    bt::Ctl* ctl_h = nullptr;     // pinned
+    double* partials_d = nullptr;
+    size_t partials_cap = 0;
+    double* mt_d = nullptr;
+    long long mt_cap = 0;
+    long long step = 0;
+    long long last_run = 0;
+    bool geometry = false;
+    dim3 grid;
+    bt::StepParams<float> pf[2];
+    bt::StepParams<double> pd[2];
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long launches = 0;
+};
+
+namespace {
+
+int fail(bt_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CK(h, call)                                                                                   \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail(h, (e_ == cudaErrorMemoryAllocation) ? BT_E_NOMEM : BT_E_CUDA,               \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                          \
+    } while (0)
+
+void drop_graphs(bt_handle* h) {
+    for (auto& g : h->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+// geometry code: bit f = in-domain solid face neighbour (-x,+x,-y,+y,-z,+z), bit 6 = pore
+__global__ void code_kernel(const uint8_t* mask, uint8_t* code, int nx, int ny, int nz) {
+    const long long n = (long long)nx * ny * nz;
+    const long long plane = (long long)nx * ny;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q % nx), y = (int)((q / nx) % ny), z = (int)(q / plane);
+        uint8_t c = 0;
+        if (mask[q]) {
+            c = bt::CODE_PORE;
+            if (x > 0 && !mask[q - 1]) c |= 1;
+            if (x < nx - 1 && !mask[q + 1]) c |= 2;
+            if (y > 0 && !mask[q - nx]) c |= 4;
+            if (y < ny - 1 && !mask[q + nx]) c |= 8;
+            if (z > 0 && !mask[q - plane]) c |= 16;
+            if (z < nz - 1 && !mask[q + plane]) c |= 32;
+        }
+        code[q] = c;
+    }
+}
+
+template <typename T>
+void fill_params(bt_handle* h, bt::StepParams<T>* p) {
+    const bt_config& c = h->cfg;
+    const double dTime = c.dt;
+    const double Bx = c.main_field[0], By = c.main_field[1], Bz = c.main_field[2];
+    double an[3];
+    if (c.scheme == BT_SCHEME_KSPACE) {
+        an[0] = 0.0; an[1] = 0.0; an[2] = 1.0;
+    } else {
+        const double anb = std::sqrt(Bx * Bx + By * By + Bz * Bz);
+        an[0] = Bx / anb; an[1] = By / anb; an[2] = Bz / anb;
+    }
+    const double D = c.d_pore;
+    for (int s = 0; s < 2; ++s) {
+        bt::StepParams<T>& P = p[s];
+        std::memset(&P, 0, sizeof(P));
+        P.nx = c.nx; P.ny = c.ny; P.nz = c.nz;
+        P.plane = (long long)c.nx * c.ny;
+        const int zsplit = (int)h->grid.z;
+        P.zchunk = (c.nz + zsplit - 1) / zsplit;
+        for (int k = 0; k < 3; ++k) {
+            P.in[k] = static_cast<const T*>(h->state[s][k]);
+            P.out[k] = static_cast<T*>(h->state[1 - s][k]);
+        }
+        P.code = h->code;
+        P.vx = static_cast<const T*>(h->vel[0]);
+        P.vy = static_cast<const T*>(h->vel[1]);
+        P.vz = static_cast<const T*>(h->vel[2]);
+        P.hx = (T)(dTime / c.dx); P.hy = (T)(dTime / c.dy); P.hz = (T)(dTime / c.dz);
+        P.hxx = (T)(dTime / (c.dx * c.dx)); P.hyy = (T)(dTime / (c.dy * c.dy)); P.hzz = (T)(dTime / (c.dz * c.dz));
+        for (int k = 0; k < 3; ++k) {
+            P.an[k] = (T)an[k];
+            P.peqn[k] = (T)(c.p_eq * an[k]);
+        }
+        P.b = (T)(dTime * c.gamma);
+        P.dx = (T)c.dx; P.dy = (T)c.dy; P.dz = (T)c.dz;
+        P.dpp = (T)(2.0 * (D * D) / (D + D + SMALL));
+        P.dps = (T)(2.0 * (SMALL * D) / (SMALL + D + SMALL));
+        // FillInDiffusinAndTime (cpp:1795-1841): bulk rate, then rho/d per solid
+        // face in the order -x, +x, -y, +y, -z, +z; tau = 1/(1/rate) as ExplicitSimple reads it
+        for (int f = 0; f < 64; ++f) {
+            double ct1 = 1.0 / c.t1, ct2 = 1.0 / c.t2;
+            const double d3[3] = {c.dx, c.dy, c.dz};
+            for (int b = 0; b < 6; ++b)
+                if (f & (1 << b)) {
+                    ct1 += c.rho1 / d3[b / 2];
+                    ct2 += c.rho2 / d3[b / 2];
+                }
+            const double tau1 = 1.0 / (1.0 / ct1), tau2 = 1.0 / (1.0 / ct2);
+            P.dtt1[f] = (T)(dTime * tau1);
+            P.dtt2[f] = (T)(dTime * tau2);
+        }
+        P.diffusion = c.diffusion ? 1 : 0;
+        P.box[0] = c.buffer[0]; P.box[1] = c.nx - c.buffer[0];
+        P.box[2] = c.buffer[1]; P.box[3] = c.ny - c.buffer[1];
+        P.box[4] = c.buffer[2]; P.box[5] = c.nz - c.buffer[2];
+        P.dxd = c.dx; P.dyd = c.dy; P.dzd = c.dz; P.gamma = c.gamma;
+        P.steps = h->steps_d;
+        P.nsched = h->nsched;
+        P.pulses = h->pulses_d;
+        P.ctl = h->ctl_d;
+        P.partials = h->partials_d;
+        P.mt = h->mt_d;
+        P.mt_cap = h->mt_cap;
+    }
+}
+
+void refresh_params(bt_handle* h) {
+    if (h->cfg.precision == BT_F64) fill_params<double>(h, h->pd);
+    else fill_params<float>(h, h->pf);
+    drop_graphs(h);
+}
+
+cudaError_t launch_one(bt_handle* h, int s) {
+    const bt_config& c = h->cfg;
+    const int prec = (c.scheme == BT_SCHEME_REFERENCE && c.vector_mult == 1) ? 1 : 0;
+    const int vel = c.velocity == 1 ? 1 : 0;
+    h->launches++;
+    if (c.precision == BT_F64) return bt::launch_step<double>(h->pd[s], c.scheme, vel, prec, h->grid, h->stream);
+    return bt::launch_step<float>(h->pf[s], c.scheme, vel, prec, h->grid, h->stream);
+}
+
+// per-step table: gradient, KSPACE wave vector and face phases, pulse ranges
+int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const double* grad_wave, long long nwave) {
+    const bt_config& c = h->cfg;
+    long long nsched = std::max<long long>(nwave, 0);
+    for (int q = 0; q < npulses; ++q) {
+        if (pulses[q].step < 0) return fail(h, BT_E_ARG, "pulse with a negative step");
+        if (c.scheme == BT_SCHEME_KSPACE && pulses[q].flag != 2)
+            return fail(h, BT_E_ARG, "the KSPACE scheme takes RF pulses (flag 2) only; gradients go in the waveform");
+        if (pulses[q].flag < 1 || pulses[q].flag > 4) return fail(h, BT_E_ARG, "pulse flag must be 1..4");
+        nsched = std::max(nsched, pulses[q].step + 1);
+    }
+    std::vector<int> order(npulses);
+    for (int q = 0; q < npulses; ++q) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pulses[a].step < pulses[b].step; });
+    std::vector<bt::DevPulse> dp(std::max(npulses, 1));
+    for (int q = 0; q < npulses; ++q) {
+        const bt_pulse& p = pulses[order[q]];
+        bt::DevPulse& d = dp[q];
+        std::memset(&d, 0, sizeof(d));
+        d.flag = p.flag;
+        d.param = p.param;
+        const double nx = p.axis[0], ny = p.axis[1], nz = p.axis[2];
+        double length = std::pow(nx * nx + ny * ny + nz * nz, 0.5);  // AddImpulse, cpp:2558-2564
+        if (length == 0.0) length = 1.0;
+        for (int k = 0; k < 3; ++k) d.axis[k] = p.axis[k];
+        d.naxis[0] = nx / length; d.naxis[1] = ny / length; d.naxis[2] = nz / length;
+        d.eff = std::pow(nx * nx + ny * ny + nz * nz, 0.5);
+    }
+    std::vector<bt::StepInfo> st(nsched + 1);
+    h->kpos.assign(3 * (nsched + 1), 0.0);
+    double k[3] = {0.0, 0.0, 0.0};
+    const double d3[3] = {c.dx, c.dy, c.dz};
+    int qi = 0;
+    for (long long s = 0; s <= nsched; ++s) {
+        bt::StepInfo& si = st[s];
+        std::memset(&si, 0, sizeof(si));
+        const bool in_wave = grad_wave && s < nwave;
+        for (int a = 0; a < 3; ++a) si.grad[a] = in_wave ? grad_wave[3 * s + a] : c.grad[a];
+        for (int a = 0; a < 3; ++a) h->kpos[3 * s + a] = k[a];
+        for (int a = 0; a < 3; ++a) {
+            // neighbour at -d: exp(+i k d); at +d: exp(-i k d)
+            const double ang = k[a] * d3[a];
+            si.phase[2 * a][0] = std::cos(ang);
+            si.phase[2 * a][1] = std::sin(ang);
+            si.phase[2 * a + 1][0] = std::cos(ang);
+            si.phase[2 * a + 1][1] = -std::sin(ang);
+        }
+        if (c.scheme == BT_SCHEME_KSPACE && s < nsched)
+            for (int a = 0; a < 3; ++a) k[a] = k[a] + c.gamma * si.grad[a] * c.dt;
+        for (int a = 0; a < 3; ++a) si.knext[a] = k[a];
+        si.pulse_first = qi;
+        while (qi < npulses && pulses[order[qi]].step == s) qi++;
+        si.pulse_count = qi - si.pulse_first;
+    }
+    // the default entry (index nsched) used beyond the table: no pulses, cfg gradient
+    {
+        bt::StepInfo& si = st[nsched];
+        for (int a = 0; a < 3; ++a) si.grad[a] = c.grad[a];
+        si.pulse_count = 0;
+    }
+    if (h->steps_d) cudaFree(h->steps_d);
+    if (h->pulses_d) cudaFree(h->pulses_d);
+    h->steps_d = nullptr;
+    h->pulses_d = nullptr;
+    CK(h, cudaMalloc(&h->steps_d, sizeof(bt::StepInfo) * st.size()));
+    CK(h, cudaMalloc(&h->pulses_d, sizeof(bt::DevPulse) * dp.size()));
+    CK(h, cudaMemcpy(h->steps_d, st.data(), sizeof(bt::StepInfo) * st.size(), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->pulses_d, dp.data(), sizeof(bt::DevPulse) * dp.size(), cudaMemcpyHostToDevice));
+    h->steps_h.swap(st);
+    h->nsched = nsched;
+    refresh_params(h);
+    return BT_OK;
+}
+
+void kvec_at(const bt_handle* h, long long s, double k[3]) {
+    if (h->cfg.scheme != BT_SCHEME_KSPACE || h->kpos.empty()) {
+        k[0] = k[1] = k[2] = 0.0;
+        return;
+    }
+    const long long i = std::min<long long>(s, h->nsched);
+    for (int a = 0; a < 3; ++a) k[a] = h->kpos[3 * i + a];
+}
+
+int ensure_mt(bt_handle* h, long long n) {
+    if (n <= h->mt_cap) return BT_OK;
+    long long cap = std::max<long long>(n, 1024);
+    if (h->mt_d) cudaFree(h->mt_d);
+    h->mt_d = nullptr;
+    h->mt_cap = 0;
+    CK(h, cudaMalloc(&h->mt_d, sizeof(double) * 3 * cap));
+    h->mt_cap = cap;
+    refresh_params(h);
+    return BT_OK;
+}
+
+int check_ctl(bt_handle* h) {
+    CK(h, cudaMemcpyAsync(h->ctl_h, h->ctl_d, sizeof(bt::Ctl), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->ctl_h->step != h->step)
+        return fail(h, BT_E_STATE, "device step counter " + std::to_string(h->ctl_h->step) + " != host " +
+                                       std::to_string(h->step));
+    if (h->ctl_h->status & 4) return fail(h, BT_E_NAN, "M(t) watchdog: a sum is NaN or Inf");
+    if (h->ctl_h->status & 1) return fail(h, BT_E_STATE, "M(t) buffer overflow");
+    return BT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bt_version(void) { return "initializator_gb300 0.1 (sm_103a)"; }
+
+int bt_create(const bt_config* cfg, bt_handle** out) {
+    if (!cfg || !out) return BT_E_ARG;
+    *out = nullptr;
+    if (cfg->nx <= 0 || cfg->ny <= 0 || cfg->nz <= 0) return BT_E_ARG;
+    if (cfg->precision != BT_F32 && cfg->precision != BT_F64) return BT_E_ARG;
+    if (cfg->scheme != BT_SCHEME_REFERENCE && cfg->scheme != BT_SCHEME_KSPACE) return BT_E_ARG;
+    if (!(cfg->dt > 0) || !(cfg->dx > 0) || !(cfg->dy > 0) || !(cfg->dz > 0)) return BT_E_ARG;
+    for (int a = 0; a < 3; ++a)
+        if (cfg->buffer[a] < 0 || 2 * cfg->buffer[a] > (a == 0 ? cfg->nx : a == 1 ? cfg->ny : cfg->nz)) return BT_E_ARG;
+    const long long nvox = (long long)cfg->nx * cfg->ny * cfg->nz;
+    if (nvox > (1LL << 40)) return BT_E_ARG;
+    bt_handle* h = new bt_handle();
+    h->cfg = *cfg;
+    h->esz = cfg->precision == BT_F64 ? 8 : 4;
+    h->nvox = (size_t)nvox;
+    int rc = BT_OK;
+    auto bail = [&](int code) {
+        bt_destroy(h);
+        return code;
+    };
+    if (cudaGetDevice(&h->device) != cudaSuccess) return bail(BT_E_CUDA);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(BT_E_CUDA);
+    // grid: 32 x 8 column tiles; z split so that the grid fills 152 SMs several times
+    const int gx = (cfg->nx + bt::TX - 1) / bt::TX, gy = (cfg->ny + bt::TY - 1) / bt::TY;
+    int zsplit = 1;
+    const long long tiles = (long long)gx * gy;
+    const long long want = 152LL * 8;
+    if (tiles < want) zsplit = (int)std::min<long long>((want + tiles - 1) / tiles, std::max(1, cfg->nz / 8));
+    if (const char* e = std::getenv("BT_ZSPLIT")) zsplit = std::max(1, std::atoi(e));
+    zsplit = std::min(zsplit, cfg->nz);
+    while ((cfg->nz + zsplit - 1) / zsplit > 1024) zsplit++;
+    h->grid = dim3(gx, gy, zsplit);
+    const size_t fbytes = h->esz * h->nvox;
+    for (int s = 0; s < 2; ++s)
+        for (int k = 0; k < 3; ++k)
+            if (cudaMalloc(&h->state[s][k], fbytes) != cudaSuccess) return bail(BT_E_NOMEM);
+    for (int s = 0; s < 2; ++s)
+        for (int k = 0; k < 3; ++k) cudaMemset(h->state[s][k], 0, fbytes);
+    if (cudaMalloc(&h->code, h->nvox) != cudaSuccess) return bail(BT_E_NOMEM);
+    cudaMemset(h->code, 0, h->nvox);
+    if (cfg->velocity == 1) {
+        const size_t nxf = (size_t)(cfg->nx + 1) * cfg->ny * cfg->nz;
+        const size_t nyf = (size_t)cfg->nx * (cfg->ny + 1) * cfg->nz;
+        const size_t nzf = (size_t)cfg->nx * cfg->ny * (cfg->nz + 1);
+        if (cudaMalloc(&h->vel[0], h->esz * nxf) != cudaSuccess) return bail(BT_E_NOMEM);
+        if (cudaMalloc(&h->vel[1], h->esz * nyf) != cudaSuccess) return bail(BT_E_NOMEM);
+        if (cudaMalloc(&h->vel[2], h->esz * nzf) != cudaSuccess) return bail(BT_E_NOMEM);
+        cudaMemset(h->vel[0], 0, h->esz * nxf);
+        cudaMemset(h->vel[1], 0, h->esz * nyf);
+        cudaMemset(h->vel[2], 0, h->esz * nzf);
+    }
+    const size_t nblocks = (size_t)h->grid.x * h->grid.y * h->grid.z;
+    h->partials_cap = std::max<size_t>(3 * nblocks, 4 * SUMS_BLOCKS);
+    if (cudaMalloc(&h->partials_d, sizeof(double) * h->partials_cap) != cudaSuccess) return bail(BT_E_NOMEM);
+    if (cudaMalloc(&h->ctl_d, sizeof(bt::Ctl)) != cudaSuccess) return bail(BT_E_NOMEM);
+    if (cudaMallocHost(&h->ctl_h, sizeof(bt::Ctl)) != cudaSuccess) return bail(BT_E_NOMEM);
+    std::memset(h->ctl_h, 0, sizeof(bt::Ctl));
+    if (cudaMemcpy(h->ctl_d, h->ctl_h, sizeof(bt::Ctl), cudaMemcpyHostToDevice) != cudaSuccess) return bail(BT_E_CUDA);
+    rc = ensure_mt(h, 1024);
+    if (rc) return bail(rc);
+    rc = build_schedule(h, nullptr, 0, nullptr, 0);
+    if (rc) return bail(rc);
+    *out = h;
+    return BT_OK;
+}
+
+int bt_destroy(bt_handle* h) {
+    if (!h) return BT_OK;
+    drop_graphs(h);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto& s : h->state)
+        for (auto& p : s)
+            if (p) cudaFree(p);
+    for (auto& p : h->vel)
+        if (p) cudaFree(p);
+    if (h->code) cudaFree(h->code);
+    if (h->steps_d) cudaFree(h->steps_d);
+    if (h->pulses_d) cudaFree(h->pulses_d);
+    if (h->ctl_d) cudaFree(h->ctl_d);
+    if (h->ctl_h) cudaFreeHost(h->ctl_h);
+    if (h->partials_d) cudaFree(h->partials_d);
+    if (h->mt_d) cudaFree(h->mt_d);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return BT_OK;
+}
+
+const char* bt_last_error(const bt_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, const double* vy, const double* vz) {
+    if (!h || !mask) return fail(h, BT_E_ARG, "mask is required");
+    const bt_config& c = h->cfg;
+    uint8_t* mtmp = nullptr;
+    CK(h, cudaMalloc(&mtmp, h->nvox));
+    cudaError_t e = cudaMemcpy(mtmp, mask, h->nvox, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        code_kernel<<<1216, 256, 0, h->stream>>>(mtmp, h->code, c.nx, c.ny, c.nz);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    }
+    cudaFree(mtmp);
+    CK(h, e);
+    if (c.velocity == 1) {
+        if (!vx || !vy || !vz) return fail(h, BT_E_ARG, "velocity == 1 needs vx, vy and vz");
+        const size_t n3[3] = {(size_t)(c.nx + 1) * c.ny * c.nz, (size_t)c.nx * (c.ny + 1) * c.nz,
+                              (size_t)c.nx * c.ny * (c.nz + 1)};
+        const double* src[3] = {vx, vy, vz};
+        for (int a = 0; a < 3; ++a) {
+            if (h->esz == 8) {
+                CK(h, cudaMemcpy(h->vel[a], src[a], 8 * n3[a], cudaMemcpyHostToDevice));
+            } else {
+                std::vector<float> f(n3[a]);
+                for (size_t q = 0; q < n3[a]; ++q) f[q] = (float)src[a][q];
+                CK(h, cudaMemcpy(h->vel[a], f.data(), 4 * n3[a], cudaMemcpyHostToDevice));
+            }
+        }
+    }
+    h->geometry = true;
+    refresh_params(h);
+    return BT_OK;
+}
+
+int bt_set_state(bt_handle* h, const double* mx, const double* my, const double* mz) {
+    if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
+    if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    const double* src[3] = {mx, my, mz};
+    std::vector<float> f;
+    if (h->esz == 4) f.resize(h->nvox);
+    for (int a = 0; a < 3; ++a) {
+        if (h->esz == 8) {
+            CK(h, cudaMemcpyAsync(h->state[h->cur][a], src[a], 8 * h->nvox, cudaMemcpyHostToDevice, h->stream));
+        } else {
+            for (size_t q = 0; q < h->nvox; ++q) f[q] = (float)src[a][q];
+            CK(h, cudaMemcpyAsync(h->state[h->cur][a], f.data(), 4 * h->nvox, cudaMemcpyHostToDevice, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+        }
+    }
+    double k[3];
+    kvec_at(h, h->step, k);
+    if (k[0] != 0.0 || k[1] != 0.0 || k[2] != 0.0) {
+        const bt_config& c = h->cfg;
+        cudaError_t e;
+        if (h->esz == 8) {
+            double* fp[3] = {(double*)h->state[h->cur][0], (double*)h->state[h->cur][1], (double*)h->state[h->cur][2]};
+            e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, +1, h->stream);
+        } else {
+            float* fp[3] = {(float*)h->state[h->cur][0], (float*)h->state[h->cur][1], (float*)h->state[h->cur][2]};
+            e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, +1, h->stream);
+        }
+        CK(h, e);
+        h->launches++;
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    return BT_OK;
+}
+
+int bt_set_state_device(bt_handle* h, const void* mx, const void* my, const void* mz) {
+    if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
+    if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    const void* src[3] = {mx, my, mz};
+    for (int a = 0; a < 3; ++a)
+        CK(h, cudaMemcpyAsync(h->state[h->cur][a], src[a], h->esz * h->nvox, cudaMemcpyDeviceToDevice, h->stream));
+    double k[3];
+    kvec_at(h, h->step, k);
+    if (k[0] != 0.0 || k[1] != 0.0 || k[2] != 0.0) {
+        const bt_config& c = h->cfg;
+        cudaError_t e;
+        if (h->esz == 8) {
+            double* fp[3] = {(double*)h->state[h->cur][0], (double*)h->state[h->cur][1], (double*)h->state[h->cur][2]};
+            e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, +1, h->stream);
+        } else {
+            float* fp[3] = {(float*)h->state[h->cur][0], (float*)h->state[h->cur][1], (float*)h->state[h->cur][2]};
+            e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, +1, h->stream);
+        }
+        CK(h, e);
+        h->launches++;
+    }
+    return BT_OK;
+}
+
+int bt_get_state(bt_handle* h, double* mx, double* my, double* mz) {
+    if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
+    const bt_config& c = h->cfg;
+    double k[3];
+    kvec_at(h, h->step, k);
+    const bool phase = (k[0] != 0.0 || k[1] != 0.0 || k[2] != 0.0);
+    // the idle ping-pong buffer holds the lab-frame copy
+    void** src = h->state[h->cur];
+    void** tmp = h->state[1 - h->cur];
+    if (phase) {
+        for (int a = 0; a < 2; ++a)
+            CK(h, cudaMemcpyAsync(tmp[a], src[a], h->esz * h->nvox, cudaMemcpyDeviceToDevice, h->stream));
+        cudaError_t e;
+        if (h->esz == 8) {
+            double* fp[3] = {(double*)tmp[0], (double*)tmp[1], (double*)tmp[2]};
+            e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, -1, h->stream);
+        } else {
+            float* fp[3] = {(float*)tmp[0], (float*)tmp[1], (float*)tmp[2]};
+            e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, -1, h->stream);
+        }
+        CK(h, e);
+        h->launches++;
+    }
+    double* dst[3] = {mx, my, mz};
+    std::vector<float> f;
+    if (h->esz == 4) f.resize(h->nvox);
+    for (int a = 0; a < 3; ++a) {
+        const void* s = (phase && a < 2) ? tmp[a] : src[a];
+        if (h->esz == 8) {
+            CK(h, cudaMemcpyAsync(dst[a], s, 8 * h->nvox, cudaMemcpyDeviceToHost, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+        } else {
+            CK(h, cudaMemcpyAsync(f.data(), s, 4 * h->nvox, cudaMemcpyDeviceToHost, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+            for (size_t q = 0; q < h->nvox; ++q) dst[a][q] = (double)f[q];
+        }
+    }
+    // the idle buffer is garbage now; the next step overwrites all of it
+    return BT_OK;
+}
+
+int bt_set_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const double* grad_wave, long long nwave) {
+    if (!h || npulses < 0 || (npulses > 0 && !pulses) || nwave < 0 || (nwave > 0 && !grad_wave))
+        return fail(h, BT_E_ARG, "bad schedule arguments");
+    CK(h, cudaStreamSynchronize(h->stream));
+    return build_schedule(h, pulses, npulses, grad_wave, nwave);
+}
+
+long long bt_step_index(const bt_handle* h) { return h ? h->step : -1; }
+
+int bt_set_step(bt_handle* h, long long step) {
+    if (!h || step < 0) return fail(h, BT_E_ARG, "bad step");
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->step = step;
+    h->ctl_h->step = step;
+    h->ctl_h->mt_base = step;
+    h->ctl_h->ticket = 0;
+    h->ctl_h->status = 0;
+    CK(h, cudaMemcpy(h->ctl_d, h->ctl_h, sizeof(bt::Ctl), cudaMemcpyHostToDevice));
+    return BT_OK;
+}
+
+int bt_run_async(bt_handle* h, long long nsteps) {
+    if (!h || nsteps < 0) return fail(h, BT_E_ARG, "bad step count");
+    if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    const bt_config& c = h->cfg;
+    if (c.scheme == BT_SCHEME_KSPACE && (c.grad[0] != 0.0 || c.grad[1] != 0.0 || c.grad[2] != 0.0) &&
+        h->step + nsteps > h->nsched)
+        return fail(h, BT_E_ARG, "KSPACE with a gradient needs a waveform covering every step run");
+    int rc = ensure_mt(h, nsteps);
+    if (rc) return rc;
+    // ctl: step and mt_base for this run (written in stream order)
+    h->ctl_h->step = h->step;
+    h->ctl_h->mt_base = h->step;
+    h->ctl_h->ticket = 0;
+    h->ctl_h->status = 0;
+    CK(h, cudaMemcpyAsync(h->ctl_d, h->ctl_h, sizeof(bt::Ctl), cudaMemcpyHostToDevice, h->stream));
+    long long left = nsteps;
+    // whole graphs of GRAPH_STEPS launches, then single launches
+    while (left >= GRAPH_STEPS) {
+        cudaGraphExec_t& g = h->graph[h->cur];
+        if (!g) {
+            cudaGraph_t graph;
+            CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = cudaSuccess;
+            const long long before = h->launches;
+            for (int q = 0; q < GRAPH_STEPS && e == cudaSuccess; ++q) e = launch_one(h, (h->cur + q) & 1);
+            h->launches = before;
+            cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+            CK(h, e);
+            CK(h, e2);
+            e = cudaGraphInstantiate(&g, graph, 0);
+            cudaGraphDestroy(graph);
+            CK(h, e);
+        }
+        CK(h, cudaGraphLaunch(g, h->stream));
+        h->launches += GRAPH_STEPS;
+        left -= GRAPH_STEPS;
+    }
+    for (long long q = 0; q < left; ++q) {
+        CK(h, launch_one(h, h->cur));
+        h->cur ^= 1;
+    }
+    h->step += nsteps;
+    h->last_run = nsteps;
+    return BT_OK;
+}
+
+int bt_read_mt(bt_handle* h, double* mt_out, long long nsteps) {
+    if (!h || nsteps < 0 || nsteps > h->last_run) return fail(h, BT_E_ARG, "bad M(t) read");
+    int rc = check_ctl(h);
+    if (rc) return rc;
+    if (mt_out && nsteps > 0)
+        CK(h, cudaMemcpy(mt_out, h->mt_d, sizeof(double) * 3 * nsteps, cudaMemcpyDeviceToHost));
+    return BT_OK;
+}
+
+int bt_run(bt_handle* h, long long nsteps, double* mt_out) {
+    int rc = bt_run_async(h, nsteps);
+    if (rc) return rc;
+    return bt_read_mt(h, mt_out, nsteps);
+}
+
+int bt_synchronize(bt_handle* h) {
+    if (!h) return BT_E_ARG;
+    CK(h, cudaStreamSynchronize(h->stream));
+    return BT_OK;
+}
+
+void* bt_stream(bt_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int bt_measure(bt_handle* h, double* sums3) {
+    if (!h || !sums3) return fail(h, BT_E_ARG, "null output");
+    if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    double kv[4];
+    kvec_at(h, h->step, kv);
+    kv[3] = SUMS_BLOCKS;
+    cudaError_t e;
+    if (h->esz == 8) e = bt::launch_sums<double>(h->pd[h->cur], kv, h->stream);
+    else e = bt::launch_sums<float>(h->pf[h->cur], kv, h->stream);
+    CK(h, e);
+    h->launches++;
+    std::vector<double> part(4 * SUMS_BLOCKS);
+    CK(h, cudaMemcpyAsync(part.data(), h->partials_d, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < SUMS_BLOCKS; ++b)
+        for (int a = 0; a < 3; ++a) t[a] += part[4 * b + a];
+    for (int a = 0; a < 3; ++a) sums3[a] = t[a];
+    return BT_OK;
+}
+
+long long bt_launch_count(const bt_handle* h) { return h ? h->launches : -1; }
+
+}  // extern "C"

@@ -1,0 +1,88 @@
+// Internal types shared by the step kernels and the host runtime.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bt {
+
+// z-marching tile: one CTA owns TX x TY columns of a z-chunk.
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int NTHREADS = TX * TY;
+constexpr int MAX_PULSES_PER_STEP = 8;
+
+// Bits of the per-voxel geometry code (one byte per voxel): bit f (0..5) is
+// set when the face neighbour f = -x,+x,-y,+y,-z,+z is an in-domain solid
+// voxel; bit 6 is set for a pore voxel. The six face bits index the 64-entry
+// relaxation-rate tables (surface relaxation rho/d per solid face).
+constexpr uint8_t CODE_PORE = 64;
+
+// Per-step schedule record (one per step, read uniformly by every CTA).
+struct StepInfo {
+    double grad[3];     // gradient during this step, T/m
+    double knext[3];    // KSPACE: wave vector after this step (rad/m)
+    double phase[6][2]; // KSPACE: face phase factor exp(-i k.(r_nb - r)) for -x,+x,-y,+y,-z,+z
+    int pulse_first;
+    int pulse_count;
+};
+
+// One pulse, with the reference's normalised axis precomputed on the host.
+struct DevPulse {
+    int flag;
+    int pad;
+    double param;
+    double axis[3];   // as given (flags 2 and 4 rotate about it)
+    double naxis[3];  // axis / |axis| (flags 1 and 3 rotate about it)
+    double eff;       // |axis| (flag 3's effective gradient)
+};
+
+// Device-side run control: the step index advances inside the kernels so a
+// captured CUDA graph can be replayed for any number of steps.
+struct Ctl {
+    long long step;      // absolute step index of the next launch
+    long long mt_base;   // step whose sums go to mt[0]
+    unsigned int ticket; // CTAs of the current launch that have finished
+    int status;          // 0 ok, 1 = M(t) buffer overflow, 2 = schedule missing
+};
+
+template <typename T>
+struct StepParams {
+    int nx, ny, nz, zchunk;
+    long long plane;            // nx * ny
+    const T* in[3];
+    T* out[3];
+    const uint8_t* code;
+    const T* vx;                // [nz][ny][nx+1]
+    const T* vy;                // [nz][ny+1][nx]
+    const T* vz;                // [nz+1][ny][nx]
+    // reference update constants, formed on the host in FP64 in the
+    // reference's operation order, then rounded to T
+    T hx, hy, hz, hxx, hyy, hzz;
+    T an[3];                    // unit main-field axis
+    T peqn[3];                  // pEq * an
+    T b;                        // dTime * g
+    T dx, dy, dz;
+    T dpp, dps;                 // harmonic-mean face diffusivity pore-pore / pore-solid
+    T dtt1[64], dtt2[64];       // dTime * (1/T1), dTime * (1/T2) per face code
+    int diffusion;
+    int box[6];                 // M(t) trimming box [x0,x1) [y0,y1) [z0,z1)
+    double dxd, dyd, dzd, gamma;  // FP64 copies for pulse angles and k phases
+    const StepInfo* steps;
+    long long nsched;           // entries in steps (steps[nsched] is the default)
+    const DevPulse* pulses;
+    Ctl* ctl;
+    double* partials;           // [gridDim x*y*z][3]
+    double* mt;                 // [mt_cap][3]
+    long long mt_cap;
+};
+
+// launchers (bt_step_f32.cu / bt_step_f64.cu)
+template <typename T>
+cudaError_t launch_step(const StepParams<T>& p, int scheme, int vel, int prec, dim3 grid, cudaStream_t s);
+template <typename T>
+cudaError_t launch_sums(const StepParams<T>& p, double* out4, cudaStream_t s);
+template <typename T>
+cudaError_t launch_frame(T* f[3], const uint8_t* code, int nx, int ny, int nz, double kx, double ky,
+                         double kz, double dx, double dy, double dz, int sign, cudaStream_t s);
+
+}  // namespace bt

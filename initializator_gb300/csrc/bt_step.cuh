@@ -1,0 +1,496 @@
+// Fused Bloch–Torrey step kernel (K1) for sm_103a.
+//
+// One launch = one explicit time step of the whole field plus its M(t) sums:
+//   relaxation (T1/T2 with surface rates from the 6 face bits of the voxel
+//   code) + precession + first-order upwind advection on face velocities +
+//   harmonic-mean 7-point diffusion, then the step's pulses, then the sum of
+//   (Mx, My, Mz) over pore voxels of the trimming box.
+//
+// Reference semantics (soleh00/Initializator):
+//   update            src/NmrRelaxationSolve.cpp:3148-3282 (ExplicitSimple)
+//   ghost layers      cpp:1664-1754 at one rank: copy -> an out-of-domain
+//                     neighbour equals the voxel itself (index clamp here)
+//   solid voxels      never updated, stay zero (cpp:3174, 2501-2506)
+//   pulses            cpp:2536-2608 (OrtTransform / AddImpulse)
+//   M(t)              cpp:3301-3461 (OutputX/Y/Z)
+// In double precision (built with -fmad=false) every expression keeps the
+// reference's operation order, so the field matches it bit for bit.
+//
+// Layout: a CTA owns TX x TY columns and marches through its z-chunk. The
+// voxel's own column rolls through registers (below / current / above); the
+// current plane plus a one-voxel x/y halo sits in shared memory. The sums
+// are accumulated per thread (Kahan-compensated in FP32, plain in FP64),
+// reduced per CTA in FP64, and the last CTA to finish adds the per-CTA
+// partials in a fixed order (deterministic), writes M(t) for the step and
+// advances the device step counter, so a captured graph replays any number
+// of steps without host involvement.
+#pragma once
+#include <cmath>
+#include "bt_internal.h"
+
+namespace bt {
+
+constexpr int SCHEME_REF = 0;
+constexpr int SCHEME_KSPACE = 1;
+constexpr int ZCHUNK_MAX = 1024;
+
+template <typename T>
+struct Acc;
+template <>
+struct Acc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        float y = v - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ double get() const { return s; }
+};
+
+// upwind switch v/(v+1e-50) (cpp:3187-3204): exactly 0 for a zero face
+// velocity, 1 otherwise (1e-50 underflows in FP32, so FP32 tests v != 0).
+__device__ __forceinline__ float upsw(float v) { return v != 0.f ? 1.f : 0.f; }
+__device__ __forceinline__ double upsw(double v) { return v / (v + 1.0e-50); }
+
+// OrtTransform (cpp:2536-2550) in FP64
+__device__ __forceinline__ void ort(double& x, double& y, double& z, double nx, double ny, double nz, double angle) {
+    double c = cos(angle), s = sin(angle);
+    double v0x = x, v0y = y, v0z = z;
+    double scal = nx * v0x + ny * v0y + nz * v0z;
+    x = v0x * c + nx * (1.0 - c) * scal + s * (ny * v0z - nz * v0y);
+    y = v0y * c + ny * (1.0 - c) * scal + s * (nz * v0x - nx * v0z);
+    z = v0z * c + nz * (1.0 - c) * scal + s * (nx * v0y - ny * v0x);
+}
+
+// AddImpulse (cpp:2552-2608) for one voxel; x, y, z are 0-based cell indices
+__device__ __forceinline__ void apply_pulse(const DevPulse& pu, double& mx, double& my, double& mz, int x, int y,
+                                            int z, double dx, double dy, double dz, double g, int nx, int ny,
+                                            int nz) {
+    const double ax = pu.axis[0], ay = pu.axis[1], az = pu.axis[2];
+    double angle;
+    if (pu.flag == 1) {
+        angle = pu.param * g * ((double)x * dx * ax + (double)y * dy * ay + (double)z * dz * az);
+        ort(mx, my, mz, pu.naxis[0], pu.naxis[1], pu.naxis[2], angle);
+    } else if (pu.flag == 2) {
+        angle = pu.param;
+        ort(mx, my, mz, ax, ay, az, angle);
+    } else if (pu.flag == 3) {
+        const double distance = 10e+12;
+        angle = g * pu.eff *
+                pow(pow(((double)(x + 1) - 1.0 - distance) * dx * pu.naxis[0] +
+                            ((double)(y + 1) - 1.0 - distance) * dy * pu.naxis[1] +
+                            ((double)(z + 1) - 1.0 - distance) * dz * pu.naxis[2],
+                        2),
+                    0.5);
+        ort(mx, my, mz, pu.naxis[0], pu.naxis[1], pu.naxis[2], angle);
+    } else if (pu.flag == 4) {
+        angle = 0.0 - g * sqrt(pow(((double)(x + 1) - 0.5) * dx * ax - 0.5 * nx * dx * ax, 2.0) +
+                               pow(((double)(y + 1) - 0.5) * dy * ay - 0.5 * ny * dy * ay, 2.0) +
+                               pow(((double)(z + 1) - 0.5) * dz * az - 0.5 * nz * dz * az, 2.0));
+        ort(mx, my, mz, ax, ay, az, angle);
+    }
+}
+
+// exp(-i * k * (c + 0.5) * d) with the argument formed and reduced in FP64
+template <typename T>
+__device__ __forceinline__ void lab_phase(double k, int c, double d, T& re, T& im) {
+    double a = k * (((double)c + 0.5) * d);
+    if constexpr (sizeof(T) == 4) {
+        const double two_pi = 6.283185307179586476925286766559;
+        a = a - two_pi * rint(a * (1.0 / two_pi));
+        float s, cs;
+        sincosf((float)a, &s, &cs);
+        re = cs;
+        im = -s;
+    } else {
+        double s, cs;
+        sincos(a, &s, &cs);
+        re = cs;
+        im = -s;
+    }
+}
+
+template <typename T, int SCHEME, bool VEL, bool PREC>
+__global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ StepParams<T> P) {
+    __shared__ T sm[3][TY + 2][TX + 2];
+    __shared__ double red[NTHREADS / 32][3];
+    __shared__ T exs[TX][2];
+    __shared__ T eys[TY][2];
+    __shared__ T ezs[SCHEME == SCHEME_KSPACE ? ZCHUNK_MAX : 1][2];
+    __shared__ int last_flag;
+
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * TX + tx;
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const int x = blockIdx.x * TX + tx;
+    const int y = blockIdx.y * TY + ty;
+    const int z0 = blockIdx.z * P.zchunk;
+    const int z1 = min(nz, z0 + P.zchunk);
+    const long long step = P.ctl->step;
+    const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched);
+    const bool inb = (x < nx) && (y < ny);
+    const int xc = min(x, nx - 1), yc = min(y, ny - 1);
+    const long long plane = P.plane;
+    const long long col = (long long)yc * nx + xc;
+    const long long vxrow = (long long)yc * (nx + 1) + xc;
+    const long long vxplane = (long long)ny * (nx + 1);
+    const long long vyplane = (long long)(ny + 1) * nx;
+
+    // per-step uniform values
+    T gdx = 0, gdy = 0, gdz = 0;
+    if constexpr (PREC && SCHEME == SCHEME_REF) {
+        gdx = (T)(si->grad[0] * P.dxd);
+        gdy = (T)(si->grad[1] * P.dyd);
+        gdz = (T)(si->grad[2] * P.dzd);
+    }
+    T ph[6][2];
+    if constexpr (SCHEME == SCHEME_KSPACE) {
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            ph[f][0] = (T)si->phase[f][0];
+            ph[f][1] = (T)si->phase[f][1];
+        }
+        // lab-frame phase tables for the frame after this step
+        if (ty == 0) lab_phase<T>(si->knext[0], x, P.dxd, exs[tx][0], exs[tx][1]);
+        if (ty == 1 && tx < TY) lab_phase<T>(si->knext[1], blockIdx.y * TY + tx, P.dyd, eys[tx][0], eys[tx][1]);
+        for (int q = tid; q < z1 - z0; q += NTHREADS) lab_phase<T>(si->knext[2], z0 + q, P.dzd, ezs[q][0], ezs[q][1]);
+        __syncthreads();
+    }
+    const int npulse = si->pulse_count;
+    const DevPulse* pulses = P.pulses + si->pulse_first;
+
+    const bool in_box = x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3];
+    Acc<T> accx, accy, accz;
+
+    // rolling column
+    T cb[3], cc[3], ca[3];
+    {
+        const long long ob = (long long)max(z0 - 1, 0) * plane + col;
+        const long long oc = (long long)z0 * plane + col;
+        const long long oa = (long long)min(z0 + 1, nz - 1) * plane + col;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            cb[c] = P.in[c][ob];
+            cc[c] = P.in[c][oc];
+            ca[c] = P.in[c][oa];
+        }
+    }
+    T wlo = 0;
+    if constexpr (VEL) wlo = P.vz[(long long)z0 * plane + col];
+
+    for (int z = z0; z < z1; ++z) {
+        // prefetch the plane after next for the rolling column
+        T nxt[3];
+        const long long on = (long long)min(z + 2, nz - 1) * plane + col;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nxt[c] = P.in[c][on];
+        const long long oz = (long long)z * plane;
+        const uint8_t cd = P.code[oz + col];
+        T um = 0, up = 0, vm = 0, vp = 0, whi = 0;
+        if constexpr (VEL) {
+            um = P.vx[(long long)z * vxplane + vxrow];
+            up = P.vx[(long long)z * vxplane + vxrow + 1];
+            vm = P.vy[(long long)z * vyplane + col];
+            vp = P.vy[(long long)z * vyplane + col + nx];
+            whi = P.vz[(long long)(z + 1) * plane + col];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sm[c][ty + 1][tx + 1] = cc[c];
+        if (tx == 0) {
+            const long long o = oz + (long long)yc * nx + max(x - 1, 0);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sm[c][ty + 1][0] = P.in[c][o];
+        }
+        if (tx == TX - 1) {
+            const long long o = oz + (long long)yc * nx + min(x + 1, nx - 1);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sm[c][ty + 1][TX + 1] = P.in[c][o];
+        }
+        if (ty == 0) {
+            const long long o = oz + (long long)max(y - 1, 0) * nx + xc;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sm[c][0][tx + 1] = P.in[c][o];
+        }
+        if (ty == TY - 1) {
+            const long long o = oz + (long long)min(y + 1, ny - 1) * nx + xc;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sm[c][TY + 1][tx + 1] = P.in[c][o];
+        }
+        __syncthreads();
+
+        if (inb) {
+            T o0 = 0, o1 = 0, o2 = 0;
+            if (cd & CODE_PORE) {
+                const int f = cd & 63;
+                const T dtt1 = P.dtt1[f], dtt2 = P.dtt2[f];
+                const T px0 = cc[0], py0 = cc[1], pz0 = cc[2];
+                // neighbours: -x +x -y +y -z +z, per component
+                T nb[3][6];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    nb[c][0] = sm[c][ty + 1][tx];
+                    nb[c][1] = sm[c][ty + 1][tx + 2];
+                    nb[c][2] = sm[c][ty][tx + 1];
+                    nb[c][3] = sm[c][ty + 2][tx + 1];
+                    nb[c][4] = cb[c];
+                    nb[c][5] = ca[c];
+                }
+                if constexpr (SCHEME == SCHEME_KSPACE) {
+                    // transverse neighbours in the frame of this voxel:
+                    // phi_f * m_nb inside the domain; the voxel itself outside
+                    // (copy ghost -> zero difference)
+                    const bool open[6] = {x > 0, x < nx - 1, y > 0, y < ny - 1, z > 0, z < nz - 1};
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) {
+                        const T re = nb[0][q], im = nb[1][q];
+                        nb[0][q] = open[q] ? ph[q][0] * re - ph[q][1] * im : px0;
+                        nb[1][q] = open[q] ? ph[q][0] * im + ph[q][1] * re : py0;
+                    }
+                }
+                T ax, ay, az;
+                if constexpr (SCHEME == SCHEME_REF) {
+                    const T div = P.an[0] * px0 + P.an[1] * py0 + P.an[2] * pz0;
+                    const T divx = P.an[0] * div, divy = P.an[1] * div, divz = P.an[2] * div;
+                    ax = px0 + dtt1 * (P.peqn[0] - divx) + dtt2 * (divx - px0);
+                    ay = py0 + dtt1 * (P.peqn[1] - divy) + dtt2 * (divy - py0);
+                    az = pz0 + dtt1 * (P.peqn[2] - divz) + dtt2 * (divz - pz0);
+                    if constexpr (PREC) {
+                        const T bbxb = P.b * (gdx * ((T)x + (T)0.5));
+                        const T bbyb = P.b * (gdy * ((T)y + (T)0.5));
+                        const T bbzb = P.b * (gdz * ((T)z + (T)0.5));
+                        ax += (T)0.0 - bbyb * pz0 + bbzb * py0;
+                        ay += (T)0.0 + bbxb * pz0 - bbzb * px0;
+                        az += (T)0.0 - bbxb * py0 + bbyb * px0;
+                    }
+                } else {
+                    // B0 along z: the reference relaxation with n = (0, 0, 1)
+                    ax = px0 + dtt2 * ((T)0.0 - px0);
+                    ay = py0 + dtt2 * ((T)0.0 - py0);
+                    az = pz0 + dtt1 * (P.peqn[2] - pz0) + dtt2 * (pz0 - pz0);
+                }
+                if constexpr (VEL) {
+                    const T upp = upsw(up), umm = upsw(um), vpp = upsw(vp), vmm = upsw(vm);
+                    const T wpp = upsw(whi), wmm = upsw(wlo);
+                    const T u = (T)0.5 * (um + up), v = (T)0.5 * (vm + vp), w = (T)0.5 * (wlo + whi);
+                    const T ud = fabs(u), vd = fabs(v), wd = fabs(w);
+                    const T hx2 = (T)0.5 * P.hx, hy2 = (T)0.5 * P.hy, hz2 = (T)0.5 * P.hz;
+                    const T p0[3] = {px0, py0, pz0};
+                    T a[3] = {ax, ay, az};
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        a[c] -= hx2 * ((u - ud) * (nb[c][1] - p0[c]) * upp + (u + ud) * (p0[c] - nb[c][0]) * umm) +
+                                hy2 * ((v - vd) * (nb[c][3] - p0[c]) * vpp + (v + vd) * (p0[c] - nb[c][2]) * vmm) +
+                                hz2 * ((w - wd) * (nb[c][5] - p0[c]) * wpp + (w + wd) * (p0[c] - nb[c][4]) * wmm);
+                    }
+                    ax = a[0];
+                    ay = a[1];
+                    az = a[2];
+                }
+                if (P.diffusion) {
+                    const T dxm = (f & 1) ? P.dps : P.dpp, dxp = (f & 2) ? P.dps : P.dpp;
+                    const T dym = (f & 4) ? P.dps : P.dpp, dyp = (f & 8) ? P.dps : P.dpp;
+                    const T dzm = (f & 16) ? P.dps : P.dpp, dzp = (f & 32) ? P.dps : P.dpp;
+                    const T p0[3] = {px0, py0, pz0};
+                    T a[3] = {ax, ay, az};
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        a[c] += P.hxx * (dxp * (nb[c][1] - p0[c]) - dxm * (p0[c] - nb[c][0])) +
+                                P.hyy * (dyp * (nb[c][3] - p0[c]) - dym * (p0[c] - nb[c][2])) +
+                                P.hzz * (dzp * (nb[c][5] - p0[c]) - dzm * (p0[c] - nb[c][4]));
+                    }
+                    ax = a[0];
+                    ay = a[1];
+                    az = a[2];
+                }
+                T lx = ax, ly = ay;  // lab-frame transverse components
+                T er = 1, ei = 0;
+                if constexpr (SCHEME == SCHEME_KSPACE) {
+                    const T exr = exs[tx][0], exi = exs[tx][1], eyr = eys[ty][0], eyi = eys[ty][1];
+                    const T ezr = ezs[z - z0][0], ezi = ezs[z - z0][1];
+                    const T xyr = exr * eyr - exi * eyi, xyi = exr * eyi + exi * eyr;
+                    er = xyr * ezr - xyi * ezi;
+                    ei = xyr * ezi + xyi * ezr;
+                    lx = er * ax - ei * ay;
+                    ly = er * ay + ei * ax;
+                }
+                if (npulse) {
+                    double mx = lx, my = ly, mz = az;
+                    for (int q = 0; q < npulse; ++q)
+                        apply_pulse(pulses[q], mx, my, mz, x, y, z, P.dxd, P.dyd, P.dzd, P.gamma, nx, ny, nz);
+                    lx = (T)mx;
+                    ly = (T)my;
+                    az = (T)mz;
+                    if constexpr (SCHEME == SCHEME_KSPACE) {
+                        ax = er * lx + ei * ly;  // back to the frame: conj(e) * lab
+                        ay = er * ly - ei * lx;
+                    } else {
+                        ax = lx;
+                        ay = ly;
+                    }
+                }
+                o0 = ax;
+                o1 = ay;
+                o2 = az;
+                if (in_box && z >= P.box[4] && z < P.box[5]) {
+                    accx.add(lx);
+                    accy.add(ly);
+                    accz.add(az);
+                }
+            }
+            P.out[0][oz + col] = o0;
+            P.out[1][oz + col] = o1;
+            P.out[2][oz + col] = o2;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            cb[c] = cc[c];
+            cc[c] = ca[c];
+            ca[c] = nxt[c];
+        }
+        if constexpr (VEL) wlo = whi;
+    }
+
+    // ---- deterministic M(t) reduction ----
+    double s3[3] = {accx.get(), accy.get(), accz.get()};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s3[c] += __shfl_down_sync(0xffffffffu, s3[c], o);
+    if ((tid & 31) == 0)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) red[tid >> 5][c] = s3[c];
+    __syncthreads();
+    const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    if (tid == 0) {
+        double t[3] = {0.0, 0.0, 0.0};
+        for (int w = 0; w < NTHREADS / 32; ++w)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) t[c] += red[w][c];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) P.partials[3ull * bid + c] = t[c];
+        __threadfence();
+        const unsigned prev = atomicAdd(&P.ctl->ticket, 1u);
+        last_flag = (prev == nblocks - 1);
+    }
+    __syncthreads();
+    if (!last_flag) return;
+    __threadfence();
+    double t[3] = {0.0, 0.0, 0.0};
+    for (unsigned q = tid; q < nblocks; q += NTHREADS)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) t[c] += __ldcg(&P.partials[3ull * q + c]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t[c] += __shfl_down_sync(0xffffffffu, t[c], o);
+    __syncthreads();
+    if ((tid & 31) == 0)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) red[tid >> 5][c] = t[c];
+    __syncthreads();
+    if (tid == 0) {
+        double u[3] = {0.0, 0.0, 0.0};
+        for (int w = 0; w < NTHREADS / 32; ++w)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) u[c] += red[w][c];
+        const long long slot = step - P.ctl->mt_base;
+        if (slot >= 0 && slot < P.mt_cap) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) P.mt[3 * slot + c] = u[c];
+        } else {
+            P.ctl->status |= 1;
+        }
+        if (!isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2])) P.ctl->status |= 4;
+        P.ctl->ticket = 0;
+        P.ctl->step = step + 1;
+        __threadfence();
+    }
+}
+
+// sums of a field (bt_measure): FP64 per thread, lab frame for a non-zero k
+template <typename T>
+__global__ void sums_kernel(const __grid_constant__ StepParams<T> P, double kx, double ky, double kz, double* out4) {
+    __shared__ double red[NTHREADS / 32][4];
+    const int tid = threadIdx.x;
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    const long long n = P.plane * P.nz;
+    const bool phase = (kx != 0.0 || ky != 0.0 || kz != 0.0);
+    for (long long q = blockIdx.x * (long long)NTHREADS + tid; q < n; q += (long long)gridDim.x * NTHREADS) {
+        if (!(P.code[q] & CODE_PORE)) continue;
+        const int x = (int)(q % P.nx), y = (int)((q / P.nx) % P.ny), z = (int)(q / P.plane);
+        if (x < P.box[0] || x >= P.box[1] || y < P.box[2] || y >= P.box[3] || z < P.box[4] || z >= P.box[5]) continue;
+        double a = (double)P.in[0][q], b = (double)P.in[1][q];
+        if (phase) {
+            double ang = kx * ((x + 0.5) * P.dxd) + ky * ((y + 0.5) * P.dyd) + kz * ((z + 0.5) * P.dzd);
+            double sn, cs;
+            sincos(ang, &sn, &cs);
+            const double ra = cs * a + sn * b, rb = cs * b - sn * a;  // exp(-i ang) * (a + i b)
+            a = ra;
+            b = rb;
+        }
+        s[0] += a;
+        s[1] += b;
+        s[2] += (double)P.in[2][q];
+        s[3] += 1.0;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+    if ((tid & 31) == 0)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) red[tid >> 5][c] = s[c];
+    __syncthreads();
+    if (tid == 0) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int w = 0; w < NTHREADS / 32; ++w)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) t[c] += red[w][c];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) P.partials[4ull * blockIdx.x + c] = t[c];
+    }
+}
+
+// frame change of the transverse field: (f0 + i f1) *= exp(sign * i * k.r)
+template <typename T>
+__global__ void frame_kernel(T* f0, T* f1, const uint8_t* code, int nx, int ny, int nz, double kx, double ky,
+                             double kz, double dx, double dy, double dz, int sign) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        if (!(code[q] & CODE_PORE)) continue;
+        const int x = (int)(q % nx), y = (int)((q / nx) % ny), z = (int)(q / ((long long)nx * ny));
+        const double ang = sign * (kx * ((x + 0.5) * dx) + ky * ((y + 0.5) * dy) + kz * ((z + 0.5) * dz));
+        double sn, cs;
+        sincos(ang, &sn, &cs);
+        const double a = (double)f0[q], b = (double)f1[q];
+        f0[q] = (T)(cs * a - sn * b);
+        f1[q] = (T)(cs * b + sn * a);
+    }
+}
+
+template <typename T>
+cudaError_t launch_step_impl(const StepParams<T>& p, int scheme, int vel, int prec, dim3 grid, cudaStream_t s) {
+    dim3 block(TX, TY);
+    if (scheme == SCHEME_REF) {
+        if (vel && prec) step_kernel<T, SCHEME_REF, true, true><<<grid, block, 0, s>>>(p);
+        else if (vel) step_kernel<T, SCHEME_REF, true, false><<<grid, block, 0, s>>>(p);
+        else if (prec) step_kernel<T, SCHEME_REF, false, true><<<grid, block, 0, s>>>(p);
+        else step_kernel<T, SCHEME_REF, false, false><<<grid, block, 0, s>>>(p);
+    } else {
+        if (vel) step_kernel<T, SCHEME_KSPACE, true, false><<<grid, block, 0, s>>>(p);
+        else step_kernel<T, SCHEME_KSPACE, false, false><<<grid, block, 0, s>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace bt

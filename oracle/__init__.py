@@ -1,0 +1,135 @@
+"""ctypes binding of the oracle (FP64 CPU restatement of the reference's update).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, where it is the checker. The product never
+imports it. ``build()`` compiles ``oracle/_build/libbt_oracle.so`` with gcc.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libbt_oracle.so")
+REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
+        ("main_field", ctypes.c_double * 3), ("gamma", ctypes.c_double), ("grad", ctypes.c_double * 3),
+        ("d_pore", ctypes.c_double), ("t1", ctypes.c_double), ("t2", ctypes.c_double),
+        ("rho1", ctypes.c_double), ("rho2", ctypes.c_double), ("p_eq", ctypes.c_double),
+        ("vector_mult", ctypes.c_int), ("velocity", ctypes.c_int), ("diffusion", ctypes.c_int),
+        ("buffer", ctypes.c_int * 3),
+    ]
+
+
+class Pulse(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_longlong), ("flag", ctypes.c_int), ("pad", ctypes.c_int),
+                ("param", ctypes.c_double), ("axis", ctypes.c_double * 3)]
+
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def build_ref() -> str | None:
+    """Compile the reference's CPU path into oracle/_ref (needs the reference sources)."""
+    if not os.path.isdir(os.environ.get("BT_REFERENCE_DIR", "/root/reference")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref",
+                    "REF=" + os.environ.get("BT_REFERENCE_DIR", "/root/reference")], check=True)
+    return REF_HARNESS
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        l = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        l.bto_run_reference.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p, dp, dp, dp, dp, dp, dp,
+                                        ctypes.c_longlong, ctypes.POINTER(Pulse), ctypes.c_int, dp, dp, ctypes.c_int]
+        l.bto_run_reference.restype = ctypes.c_int
+        l.bto_sums.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p, dp, dp, dp, dp]
+        l.bto_sums.restype = ctypes.c_longlong
+        l.bto_rates.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p, dp, dp]
+        l.bto_last_loop_seconds.argtypes = []
+        l.bto_last_loop_seconds.restype = ctypes.c_double
+        _lib = l
+    return _lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_params(shape, *, dx, dy=None, dz=None, dt, main_field=(1.0, 0.0, 0.0), gamma=4.78941714e7,
+                grad=(0.0, 0.0, 0.0), d_pore=2.3e-9, t1=2.5, t2=2.0, rho1=0.0, rho2=0.0, p_eq=1.0,
+                vector_mult=0, velocity=0, diffusion=1, buffer=(0, 0, 0)) -> Params:
+    nz, ny, nx = shape
+    p = Params()
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.dx = dx
+    p.dy = dx if dy is None else dy
+    p.dz = dx if dz is None else dz
+    p.dt = dt
+    p.main_field[:] = list(main_field)
+    p.gamma = gamma
+    p.grad[:] = list(grad)
+    p.d_pore, p.t1, p.t2, p.rho1, p.rho2, p.p_eq = d_pore, t1, t2, rho1, rho2, p_eq
+    p.vector_mult, p.velocity, p.diffusion = vector_mult, velocity, diffusion
+    p.buffer[:] = list(buffer)
+    return p
+
+
+def run(params: Params, mask, state, nsteps, vel=None, pulses=(), grad_wave=None, threads=0):
+    """Advance ``state`` (3, nz, ny, nx) float64 by nsteps; returns (state, mt[nsteps, 3])."""
+    mask = np.ascontiguousarray(mask, dtype=np.uint8)
+    st = np.array(state, dtype=np.float64, copy=True)
+    mx, my, mz = (np.ascontiguousarray(st[c]) for c in range(3))
+    vx = vy = vz = None
+    if vel is not None:
+        vx, vy, vz = (np.ascontiguousarray(v, dtype=np.float64) for v in vel)
+    parr = (Pulse * max(1, len(pulses)))()
+    for n, (step, flag, param, axis) in enumerate(pulses):
+        parr[n].step, parr[n].flag, parr[n].param = step, flag, param
+        parr[n].axis[:] = list(axis)
+    gw = None if grad_wave is None else np.ascontiguousarray(grad_wave, dtype=np.float64)
+    mt = np.zeros((max(nsteps, 1), 3), dtype=np.float64)
+    rc = lib().bto_run_reference(ctypes.byref(params), mask.ctypes.data, _dp(vx), _dp(vy), _dp(vz),
+                                 _dp(mx), _dp(my), _dp(mz), nsteps, parr, len(pulses), _dp(gw), _dp(mt), threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle failed: {rc}")
+    return np.stack([mx, my, mz]), mt[:nsteps]
+
+
+def last_loop_seconds() -> float:
+    """Stepping-loop wall time of the last run() (array set-up excluded)."""
+    return float(lib().bto_last_loop_seconds())
+
+
+def sums(params: Params, mask, state):
+    mask = np.ascontiguousarray(mask, dtype=np.uint8)
+    mx, my, mz = (np.ascontiguousarray(state[c], dtype=np.float64) for c in range(3))
+    out = np.zeros(3)
+    n = lib().bto_sums(ctypes.byref(params), mask.ctypes.data, _dp(mx), _dp(my), _dp(mz), _dp(out))
+    return out, int(n)
+
+
+def rates(params: Params, mask):
+    mask = np.ascontiguousarray(mask, dtype=np.uint8)
+    t1 = np.zeros(mask.shape)
+    t2 = np.zeros(mask.shape)
+    lib().bto_rates(ctypes.byref(params), mask.ctypes.data, _dp(t1), _dp(t2))
+    return t1, t2
