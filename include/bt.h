@@ -135,6 +135,12 @@ void* bt_stream(bt_handle* h);
 /* M(t) sums of the current field (OutputX/Y/Z, cpp:3301-3461). */
 int bt_measure(bt_handle* h, double* sums3);
 
+/* Pick the z-chunking of the FP32 fast path by timing trial_steps steps for
+ * each candidate split (no reference counterpart: the reference launches one
+ * thread per voxel, cu:1475-1476). The field and step index are restored.
+ * *best_zsplit (may be NULL) receives the chosen split. */
+int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit);
+
 /* Number of kernel launches this handle has issued (a launch inside a replayed
  * CUDA graph counts once per replay). */
 long long bt_launch_count(const bt_handle* h);

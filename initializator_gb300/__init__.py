@@ -60,7 +60,7 @@ EXPORTS = [
     "bt_create", "bt_destroy", "bt_last_error", "bt_upload_geometry", "bt_set_state", "bt_get_state",
     "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
     "bt_read_mt", "bt_synchronize", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
-    "bt_version",
+    "bt_version", "bt_autotune",
 ]
 
 _lib = None
@@ -97,6 +97,7 @@ def lib():
         "bt_sequence_schedule": ([ctypes.POINTER(SequenceParams), ll, ctypes.POINTER(Pulse), i,
                                   ctypes.POINTER(ctypes.c_int)], i),
         "bt_version": ([], ctypes.c_char_p),
+        "bt_autotune": ([vp, i, ctypes.POINTER(ctypes.c_int)], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(l, name)
@@ -251,6 +252,12 @@ class Solver:
         out = np.zeros(3)
         self._check(self._l.bt_measure(self._h, _dp(out)), "measure")
         return out
+
+    def autotune(self, trial_steps=64):
+        """Time the candidate z-splits of the FP32 fast path; returns the chosen one."""
+        best = ctypes.c_int(0)
+        self._check(self._l.bt_autotune(self._h, int(trial_steps), ctypes.byref(best)), "autotune")
+        return best.value
 
     @property
     def launches(self):

@@ -1,8 +1,16 @@
 // Host runtime behind include/bt.h: handles, device memory, the per-step
-// schedule table and the CUDA-graph-replayed step loop.
+// schedule table, kernel selection and the CUDA-graph-replayed step loop.
+//
+// Kernel selection per step: FP32 steps without pulses run the TMA fast path
+// (bt_step_tma.cuh); FP64 steps and steps carrying pulses run the generic
+// fused kernel (bt_step.cuh). Runs of GRAPH_STEPS pulse-free steps are
+// replayed from a captured CUDA graph (the step index lives on the device).
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -13,27 +21,30 @@
 namespace {
 
 constexpr double SMALL = 1.0e-50;
-constexpr int GRAPH_STEPS = 32;   // steps per captured graph (even: state returns to the same buffer)
+constexpr int GRAPH_STEPS = 32;   // steps per captured graph (even: the state returns to the same buffer)
 constexpr int SUMS_BLOCKS = 1216; // 152 SMs x 8
+constexpr int NUM_SMS_GB300 = 152;
 
-struct Dev {
-    void* p = nullptr;
-    size_t n = 0;
-};
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
 }  // namespace
 
 struct bt_handle {
     bt_config cfg{};
     int device = 0;
+    int num_sms = NUM_SMS_GB300;
     cudaStream_t stream = nullptr;
     std::string err;
     size_t esz = 4;               // element size of the fields
-    size_t nvox = 0;
+    size_t nvox = 0;              // nx*ny*nz
+    int pitch = 0, vxpitch = 0, cpitch = 0;
+    size_t comp = 0;              // elements per component (pitch*ny*nz)
+    void* state_base[2] = {};     // one allocation of 3 components per ping-pong side
     void* state[2][3] = {};
     int cur = 0;
     uint8_t* code = nullptr;
     void* vel[3] = {};
+    void* staging = nullptr;      // pinned host buffer, one component in the handle's precision
     bt::StepInfo* steps_d = nullptr;
     long long nsched = 0;
     std::vector<bt::StepInfo> steps_h;
@@ -48,9 +59,13 @@ struct bt_handle {
     long long step = 0;
     long long last_run = 0;
     bool geometry = false;
-    dim3 grid;
+    bool use_tma = false;
+    dim3 grid;                    // generic kernel grid
+    dim3 tgrid;                   // TMA kernel grid (zsplit, x tiles, y tiles)
     bt::StepParams<float> pf[2];
     bt::StepParams<double> pd[2];
+    bt::StepParams<float> pt[2];  // TMA path (own z-chunking)
+    bt::TmaMaps maps[2];
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long launches = 0;
 };
@@ -79,7 +94,7 @@ void drop_graphs(bt_handle* h) {
 }
 
 // geometry code: bit f = in-domain solid face neighbour (-x,+x,-y,+y,-z,+z), bit 6 = pore
-__global__ void code_kernel(const uint8_t* mask, uint8_t* code, int nx, int ny, int nz) {
+__global__ void code_kernel(const uint8_t* mask, uint8_t* code, int nx, int ny, int nz, int cpitch) {
     const long long n = (long long)nx * ny * nz;
     const long long plane = (long long)nx * ny;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
@@ -94,12 +109,12 @@ __global__ void code_kernel(const uint8_t* mask, uint8_t* code, int nx, int ny, 
             if (z > 0 && !mask[q - plane]) c |= 16;
             if (z < nz - 1 && !mask[q + plane]) c |= 32;
         }
-        code[q] = c;
+        code[((long long)z * ny + y) * cpitch + x] = c;
     }
 }
 
 template <typename T>
-void fill_params(bt_handle* h, bt::StepParams<T>* p) {
+void fill_params(bt_handle* h, bt::StepParams<T>* p, dim3 grid) {
     const bt_config& c = h->cfg;
     const double dTime = c.dt;
     const double Bx = c.main_field[0], By = c.main_field[1], Bz = c.main_field[2];
@@ -115,9 +130,10 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p) {
         bt::StepParams<T>& P = p[s];
         std::memset(&P, 0, sizeof(P));
         P.nx = c.nx; P.ny = c.ny; P.nz = c.nz;
-        P.plane = (long long)c.nx * c.ny;
-        const int zsplit = (int)h->grid.z;
-        P.zchunk = (c.nz + zsplit - 1) / zsplit;
+        P.pitch = h->pitch; P.vxpitch = h->vxpitch; P.cpitch = h->cpitch;
+        P.plane = (long long)h->pitch * c.ny;
+        P.zsplit = (int)grid.z;
+        P.zchunk = (c.nz + P.zsplit - 1) / P.zsplit;
         for (int k = 0; k < 3; ++k) {
             P.in[k] = static_cast<const T*>(h->state[s][k]);
             P.out[k] = static_cast<T*>(h->state[1 - s][k]);
@@ -166,18 +182,121 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p) {
 }
 
 void refresh_params(bt_handle* h) {
-    if (h->cfg.precision == BT_F64) fill_params<double>(h, h->pd);
-    else fill_params<float>(h, h->pf);
+    if (h->cfg.precision == BT_F64) {
+        fill_params<double>(h, h->pd, h->grid);
+    } else {
+        fill_params<float>(h, h->pf, h->grid);
+        fill_params<float>(h, h->pt, dim3(1, 1, h->tgrid.x));
+    }
     drop_graphs(h);
 }
 
-cudaError_t launch_one(bt_handle* h, int s) {
+PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+bool encode(CUtensorMap* m, CUtensorMapDataType t, int rank, void* base, const cuuint64_t* dims,
+            const cuuint64_t* strides, const cuuint32_t* box) {
+    auto fn = encoder();
+    if (!fn) return false;
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    return fn(m, t, rank, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// tensor maps of the FP32 fast path; false leaves the generic kernel in charge
+bool build_maps(bt_handle* h) {
+    const bt_config& c = h->cfg;
+    const cuuint64_t nx = c.nx, ny = c.ny, nz = c.nz;
+    const cuuint64_t P4 = (cuuint64_t)h->pitch * 4, V4 = (cuuint64_t)h->vxpitch * 4;
+    for (int s = 0; s < 2; ++s) {
+        bt::TmaMaps& M = h->maps[s];
+        std::memset(&M, 0, sizeof(M));
+        {
+            cuuint64_t dims[4] = {nx, ny, nz, 3};
+            cuuint64_t str[3] = {P4, P4 * ny, (cuuint64_t)h->comp * 4};
+            cuuint32_t box[4] = {bt::TMA_TX + 8, bt::TMA_TY + 2, 1, 3};
+            if (!encode(&M.state, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->state_base[s], dims, str, box)) return false;
+        }
+        {
+            cuuint64_t dims[3] = {nx, ny, nz};
+            cuuint64_t str[2] = {(cuuint64_t)h->cpitch, (cuuint64_t)h->cpitch * ny};
+            cuuint32_t box[3] = {bt::TMA_TX, bt::TMA_TY, 1};
+            if (!encode(&M.code, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, h->code, dims, str, box)) return false;
+        }
+        if (c.velocity == 1) {
+            cuuint64_t dx_[3] = {nx + 1, ny, nz}, sx[2] = {V4, V4 * ny};
+            cuuint32_t bx[3] = {bt::TMA_TX + 4, bt::TMA_TY, 1};
+            if (!encode(&M.vx, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->vel[0], dx_, sx, bx)) return false;
+            cuuint64_t dy_[3] = {nx, ny + 1, nz}, sy[2] = {P4, P4 * (ny + 1)};
+            cuuint32_t by[3] = {bt::TMA_TX, bt::TMA_TY + 1, 1};
+            if (!encode(&M.vy, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->vel[1], dy_, sy, by)) return false;
+            cuuint64_t dz_[3] = {nx, ny, nz + 1}, sz[2] = {P4, P4 * ny};
+            cuuint32_t bz[3] = {bt::TMA_TX, bt::TMA_TY, 1};
+            if (!encode(&M.vz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->vel[2], dz_, sz, bz)) return false;
+        }
+    }
+    return true;
+}
+
+// z-chunking with no empty chunk: zsplit = ceil(nz / zchunk)
+int normalise_split(int nz, int zsplit) {
+    zsplit = std::max(1, std::min(zsplit, nz));
+    while ((nz + zsplit - 1) / zsplit > 1024) zsplit++;
+    const int zchunk = (nz + zsplit - 1) / zsplit;
+    return (nz + zchunk - 1) / zchunk;
+}
+
+int set_tma_split(bt_handle* h, int zsplit) {
+    const bt_config& c = h->cfg;
+    zsplit = normalise_split(c.nz, zsplit);
+    const int gx = (c.nx + bt::TMA_TX - 1) / bt::TMA_TX, gy = (c.ny + bt::TMA_TY - 1) / bt::TMA_TY;
+    h->tgrid = dim3(zsplit, gx, gy);
+    const size_t need = 3 * (size_t)zsplit * gx * gy;
+    if (need > h->partials_cap) {
+        if (h->partials_d) cudaFree(h->partials_d);
+        h->partials_d = nullptr;
+        h->partials_cap = 0;
+        CK(h, cudaMalloc(&h->partials_d, sizeof(double) * need));
+        h->partials_cap = need;
+    }
+    refresh_params(h);
+    return BT_OK;
+}
+
+// default split: about 4 waves of 2 CTAs per SM, chunks of at least 8 planes
+int default_tma_split(const bt_handle* h) {
+    const bt_config& c = h->cfg;
+    const long long tiles = (long long)((c.nx + bt::TMA_TX - 1) / bt::TMA_TX) * ((c.ny + bt::TMA_TY - 1) / bt::TMA_TY);
+    const long long slots = 2LL * h->num_sms;
+    long long zs = (4 * slots + tiles - 1) / tiles;
+    zs = std::min<long long>(zs, std::max(1, c.nz / 8));
+    if (const char* e = std::getenv("BT_TMA_ZSPLIT")) zs = std::max(1, std::atoi(e));
+    return (int)std::max<long long>(1, zs);
+}
+
+bool step_has_pulse(const bt_handle* h, long long s) {
+    return s < h->nsched && h->steps_h[s].pulse_count > 0;
+}
+
+cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
     const bt_config& c = h->cfg;
     const int prec = (c.scheme == BT_SCHEME_REFERENCE && c.vector_mult == 1) ? 1 : 0;
     const int vel = c.velocity == 1 ? 1 : 0;
     h->launches++;
-    if (c.precision == BT_F64) return bt::launch_step<double>(h->pd[s], c.scheme, vel, prec, h->grid, h->stream);
-    return bt::launch_step<float>(h->pf[s], c.scheme, vel, prec, h->grid, h->stream);
+    if (c.precision == BT_F64) return bt::launch_step<double>(h->pd[side], c.scheme, vel, prec, h->grid, h->stream);
+    if (h->use_tma && !step_has_pulse(h, abs_step))
+        return bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, h->stream);
+    return bt::launch_step<float>(h->pf[side], c.scheme, vel, prec, h->grid, h->stream);
 }
 
 // per-step table: gradient, KSPACE wave vector and face phases, pulse ranges
@@ -232,14 +351,10 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
         for (int a = 0; a < 3; ++a) si.knext[a] = k[a];
         si.pulse_first = qi;
         while (qi < npulses && pulses[order[qi]].step == s) qi++;
-        si.pulse_count = qi - si.pulse_first;
+        si.pulse_count = s < nsched ? qi - si.pulse_first : 0;
     }
     // the default entry (index nsched) used beyond the table: no pulses, cfg gradient
-    {
-        bt::StepInfo& si = st[nsched];
-        for (int a = 0; a < 3; ++a) si.grad[a] = c.grad[a];
-        si.pulse_count = 0;
-    }
+    for (int a = 0; a < 3; ++a) st[nsched].grad[a] = c.grad[a];
     if (h->steps_d) cudaFree(h->steps_d);
     if (h->pulses_d) cudaFree(h->pulses_d);
     h->steps_d = nullptr;
@@ -278,6 +393,7 @@ int ensure_mt(bt_handle* h, long long n) {
 int check_ctl(bt_handle* h) {
     CK(h, cudaMemcpyAsync(h->ctl_h, h->ctl_d, sizeof(bt::Ctl), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    if (h->ctl_h->status & 8) return fail(h, BT_E_TIMEOUT, "a bounded device wait (TMA mbarrier) gave up");
     if (h->ctl_h->step != h->step)
         return fail(h, BT_E_STATE, "device step counter " + std::to_string(h->ctl_h->step) + " != host " +
                                        std::to_string(h->step));
@@ -286,11 +402,61 @@ int check_ctl(bt_handle* h) {
     return BT_OK;
 }
 
+int frame_change(bt_handle* h, void* const* f, int sign) {
+    double k[3];
+    kvec_at(h, h->step, k);
+    if (k[0] == 0.0 && k[1] == 0.0 && k[2] == 0.0) return BT_OK;
+    const bt_config& c = h->cfg;
+    cudaError_t e;
+    if (h->esz == 8) {
+        double* fp[3] = {(double*)f[0], (double*)f[1], (double*)f[2]};
+        e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, h->pitch, h->cpitch, k[0], k[1], k[2], c.dx, c.dy,
+                                     c.dz, sign, h->stream);
+    } else {
+        float* fp[3] = {(float*)f[0], (float*)f[1], (float*)f[2]};
+        e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, h->pitch, h->cpitch, k[0], k[1], k[2], c.dx, c.dy,
+                                    c.dz, sign, h->stream);
+    }
+    CK(h, e);
+    h->launches++;
+    return BT_OK;
+}
+
+// dense [nz][ny][nx] host component <-> pitched device component
+int put_component(bt_handle* h, void* dst, const double* src) {
+    const bt_config& c = h->cfg;
+    const size_t rows = (size_t)c.ny * c.nz;
+    if (h->esz == 8) {
+        CK(h, cudaMemcpy2DAsync(dst, h->pitch * 8, src, c.nx * 8, c.nx * 8, rows, cudaMemcpyHostToDevice, h->stream));
+    } else {
+        CK(h, cudaStreamSynchronize(h->stream));  // the staging buffer may still feed a copy
+        float* f = static_cast<float*>(h->staging);
+        for (size_t q = 0; q < h->nvox; ++q) f[q] = (float)src[q];
+        CK(h, cudaMemcpy2DAsync(dst, h->pitch * 4, f, c.nx * 4, c.nx * 4, rows, cudaMemcpyHostToDevice, h->stream));
+    }
+    return BT_OK;
+}
+
+int get_component(bt_handle* h, double* dst, const void* src) {
+    const bt_config& c = h->cfg;
+    const size_t rows = (size_t)c.ny * c.nz;
+    if (h->esz == 8) {
+        CK(h, cudaMemcpy2DAsync(dst, c.nx * 8, src, h->pitch * 8, c.nx * 8, rows, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    } else {
+        float* f = static_cast<float*>(h->staging);
+        CK(h, cudaMemcpy2DAsync(f, c.nx * 4, src, h->pitch * 4, c.nx * 4, rows, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        for (size_t q = 0; q < h->nvox; ++q) dst[q] = (double)f[q];
+    }
+    return BT_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
-const char* bt_version(void) { return "initializator_gb300 0.1 (sm_103a)"; }
+const char* bt_version(void) { return "initializator_gb300 0.2 (sm_103a)"; }
 
 int bt_create(const bt_config* cfg, bt_handle** out) {
     if (!cfg || !out) return BT_E_ARG;
@@ -302,47 +468,50 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     for (int a = 0; a < 3; ++a)
         if (cfg->buffer[a] < 0 || 2 * cfg->buffer[a] > (a == 0 ? cfg->nx : a == 1 ? cfg->ny : cfg->nz)) return BT_E_ARG;
     const long long nvox = (long long)cfg->nx * cfg->ny * cfg->nz;
-    if (nvox > (1LL << 40)) return BT_E_ARG;
+    if (nvox > (1LL << 40) || cfg->nx > (1 << 28) || cfg->ny > (1 << 28)) return BT_E_ARG;
     bt_handle* h = new bt_handle();
     h->cfg = *cfg;
     h->esz = cfg->precision == BT_F64 ? 8 : 4;
     h->nvox = (size_t)nvox;
+    h->pitch = round_up(cfg->nx, 4);
+    h->vxpitch = round_up(cfg->nx + 1, 4);
+    h->cpitch = round_up(cfg->nx, 16);
+    h->comp = (size_t)h->pitch * cfg->ny * cfg->nz;
     int rc = BT_OK;
     auto bail = [&](int code) {
         bt_destroy(h);
         return code;
     };
     if (cudaGetDevice(&h->device) != cudaSuccess) return bail(BT_E_CUDA);
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(BT_E_CUDA);
-    // grid: 32 x 8 column tiles; z split so that the grid fills 152 SMs several times
+    // generic kernel grid: 32 x 8 column tiles; z split so that the grid fills the SMs several times
     const int gx = (cfg->nx + bt::TX - 1) / bt::TX, gy = (cfg->ny + bt::TY - 1) / bt::TY;
     int zsplit = 1;
     const long long tiles = (long long)gx * gy;
-    const long long want = 152LL * 8;
+    const long long want = 8LL * h->num_sms;
     if (tiles < want) zsplit = (int)std::min<long long>((want + tiles - 1) / tiles, std::max(1, cfg->nz / 8));
     if (const char* e = std::getenv("BT_ZSPLIT")) zsplit = std::max(1, std::atoi(e));
-    zsplit = std::min(zsplit, cfg->nz);
-    while ((cfg->nz + zsplit - 1) / zsplit > 1024) zsplit++;
+    zsplit = normalise_split(cfg->nz, zsplit);
     h->grid = dim3(gx, gy, zsplit);
-    const size_t fbytes = h->esz * h->nvox;
-    for (int s = 0; s < 2; ++s)
-        for (int k = 0; k < 3; ++k)
-            if (cudaMalloc(&h->state[s][k], fbytes) != cudaSuccess) return bail(BT_E_NOMEM);
-    for (int s = 0; s < 2; ++s)
-        for (int k = 0; k < 3; ++k) cudaMemset(h->state[s][k], 0, fbytes);
-    if (cudaMalloc(&h->code, h->nvox) != cudaSuccess) return bail(BT_E_NOMEM);
-    cudaMemset(h->code, 0, h->nvox);
-    if (cfg->velocity == 1) {
-        const size_t nxf = (size_t)(cfg->nx + 1) * cfg->ny * cfg->nz;
-        const size_t nyf = (size_t)cfg->nx * (cfg->ny + 1) * cfg->nz;
-        const size_t nzf = (size_t)cfg->nx * cfg->ny * (cfg->nz + 1);
-        if (cudaMalloc(&h->vel[0], h->esz * nxf) != cudaSuccess) return bail(BT_E_NOMEM);
-        if (cudaMalloc(&h->vel[1], h->esz * nyf) != cudaSuccess) return bail(BT_E_NOMEM);
-        if (cudaMalloc(&h->vel[2], h->esz * nzf) != cudaSuccess) return bail(BT_E_NOMEM);
-        cudaMemset(h->vel[0], 0, h->esz * nxf);
-        cudaMemset(h->vel[1], 0, h->esz * nyf);
-        cudaMemset(h->vel[2], 0, h->esz * nzf);
+    const size_t sbytes = 3 * h->esz * h->comp;
+    for (int s = 0; s < 2; ++s) {
+        if (cudaMalloc(&h->state_base[s], sbytes) != cudaSuccess) return bail(BT_E_NOMEM);
+        cudaMemset(h->state_base[s], 0, sbytes);
+        for (int k = 0; k < 3; ++k) h->state[s][k] = static_cast<char*>(h->state_base[s]) + k * h->esz * h->comp;
     }
+    const size_t cbytes = (size_t)h->cpitch * cfg->ny * cfg->nz;
+    if (cudaMalloc(&h->code, cbytes) != cudaSuccess) return bail(BT_E_NOMEM);
+    cudaMemset(h->code, 0, cbytes);
+    if (cfg->velocity == 1) {
+        const size_t n3[3] = {(size_t)h->vxpitch * cfg->ny * cfg->nz, (size_t)h->pitch * (cfg->ny + 1) * cfg->nz,
+                              (size_t)h->pitch * cfg->ny * (cfg->nz + 1)};
+        for (int a = 0; a < 3; ++a) {
+            if (cudaMalloc(&h->vel[a], h->esz * n3[a]) != cudaSuccess) return bail(BT_E_NOMEM);
+            cudaMemset(h->vel[a], 0, h->esz * n3[a]);
+        }
+    }
+    if (cfg->precision == BT_F32 && cudaMallocHost(&h->staging, 4 * h->nvox) != cudaSuccess) return bail(BT_E_NOMEM);
     const size_t nblocks = (size_t)h->grid.x * h->grid.y * h->grid.z;
     h->partials_cap = std::max<size_t>(3 * nblocks, 4 * SUMS_BLOCKS);
     if (cudaMalloc(&h->partials_d, sizeof(double) * h->partials_cap) != cudaSuccess) return bail(BT_E_NOMEM);
@@ -350,10 +519,15 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     if (cudaMallocHost(&h->ctl_h, sizeof(bt::Ctl)) != cudaSuccess) return bail(BT_E_NOMEM);
     std::memset(h->ctl_h, 0, sizeof(bt::Ctl));
     if (cudaMemcpy(h->ctl_d, h->ctl_h, sizeof(bt::Ctl), cudaMemcpyHostToDevice) != cudaSuccess) return bail(BT_E_CUDA);
+    h->tgrid = dim3(1, 1, 1);
     rc = ensure_mt(h, 1024);
     if (rc) return bail(rc);
     rc = build_schedule(h, nullptr, 0, nullptr, 0);
     if (rc) return bail(rc);
+    if (cfg->precision == BT_F32 && !std::getenv("BT_NO_TMA")) {
+        rc = set_tma_split(h, default_tma_split(h));
+        if (rc) return bail(rc);
+    }
     *out = h;
     return BT_OK;
 }
@@ -362,9 +536,8 @@ int bt_destroy(bt_handle* h) {
     if (!h) return BT_OK;
     drop_graphs(h);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    for (auto& s : h->state)
-        for (auto& p : s)
-            if (p) cudaFree(p);
+    for (auto& p : h->state_base)
+        if (p) cudaFree(p);
     for (auto& p : h->vel)
         if (p) cudaFree(p);
     if (h->code) cudaFree(h->code);
@@ -372,6 +545,7 @@ int bt_destroy(bt_handle* h) {
     if (h->pulses_d) cudaFree(h->pulses_d);
     if (h->ctl_d) cudaFree(h->ctl_d);
     if (h->ctl_h) cudaFreeHost(h->ctl_h);
+    if (h->staging) cudaFreeHost(h->staging);
     if (h->partials_d) cudaFree(h->partials_d);
     if (h->mt_d) cudaFree(h->mt_d);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -384,32 +558,37 @@ const char* bt_last_error(const bt_handle* h) { return h ? h->err.c_str() : "nul
 int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, const double* vy, const double* vz) {
     if (!h || !mask) return fail(h, BT_E_ARG, "mask is required");
     const bt_config& c = h->cfg;
+    if (c.velocity == 1 && (!vx || !vy || !vz)) return fail(h, BT_E_ARG, "velocity == 1 needs vx, vy and vz");
     uint8_t* mtmp = nullptr;
     CK(h, cudaMalloc(&mtmp, h->nvox));
     cudaError_t e = cudaMemcpy(mtmp, mask, h->nvox, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        code_kernel<<<1216, 256, 0, h->stream>>>(mtmp, h->code, c.nx, c.ny, c.nz);
+        code_kernel<<<1216, 256, 0, h->stream>>>(mtmp, h->code, c.nx, c.ny, c.nz, h->cpitch);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     }
     cudaFree(mtmp);
     CK(h, e);
     if (c.velocity == 1) {
-        if (!vx || !vy || !vz) return fail(h, BT_E_ARG, "velocity == 1 needs vx, vy and vz");
-        const size_t n3[3] = {(size_t)(c.nx + 1) * c.ny * c.nz, (size_t)c.nx * (c.ny + 1) * c.nz,
-                              (size_t)c.nx * c.ny * (c.nz + 1)};
+        // dense [k][j][i] faces -> pitched rows
+        const int w3[3] = {c.nx + 1, c.nx, c.nx};
+        const int p3[3] = {h->vxpitch, h->pitch, h->pitch};
+        const size_t rows3[3] = {(size_t)c.ny * c.nz, (size_t)(c.ny + 1) * c.nz, (size_t)c.ny * (c.nz + 1)};
         const double* src[3] = {vx, vy, vz};
         for (int a = 0; a < 3; ++a) {
+            const size_t n = (size_t)w3[a] * rows3[a];
             if (h->esz == 8) {
-                CK(h, cudaMemcpy(h->vel[a], src[a], 8 * n3[a], cudaMemcpyHostToDevice));
+                CK(h, cudaMemcpy2D(h->vel[a], p3[a] * 8, src[a], w3[a] * 8, w3[a] * 8, rows3[a], cudaMemcpyHostToDevice));
             } else {
-                std::vector<float> f(n3[a]);
-                for (size_t q = 0; q < n3[a]; ++q) f[q] = (float)src[a][q];
-                CK(h, cudaMemcpy(h->vel[a], f.data(), 4 * n3[a], cudaMemcpyHostToDevice));
+                std::vector<float> f(n);
+                for (size_t q = 0; q < n; ++q) f[q] = (float)src[a][q];
+                CK(h, cudaMemcpy2D(h->vel[a], p3[a] * 4, f.data(), w3[a] * 4, w3[a] * 4, rows3[a],
+                                   cudaMemcpyHostToDevice));
             }
         }
     }
     h->geometry = true;
+    if (h->cfg.precision == BT_F32 && h->tgrid.y > 0 && !std::getenv("BT_NO_TMA")) h->use_tma = build_maps(h);
     refresh_params(h);
     return BT_OK;
 }
@@ -418,32 +597,12 @@ int bt_set_state(bt_handle* h, const double* mx, const double* my, const double*
     if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
     const double* src[3] = {mx, my, mz};
-    std::vector<float> f;
-    if (h->esz == 4) f.resize(h->nvox);
     for (int a = 0; a < 3; ++a) {
-        if (h->esz == 8) {
-            CK(h, cudaMemcpyAsync(h->state[h->cur][a], src[a], 8 * h->nvox, cudaMemcpyHostToDevice, h->stream));
-        } else {
-            for (size_t q = 0; q < h->nvox; ++q) f[q] = (float)src[a][q];
-            CK(h, cudaMemcpyAsync(h->state[h->cur][a], f.data(), 4 * h->nvox, cudaMemcpyHostToDevice, h->stream));
-            CK(h, cudaStreamSynchronize(h->stream));
-        }
+        int rc = put_component(h, h->state[h->cur][a], src[a]);
+        if (rc) return rc;
     }
-    double k[3];
-    kvec_at(h, h->step, k);
-    if (k[0] != 0.0 || k[1] != 0.0 || k[2] != 0.0) {
-        const bt_config& c = h->cfg;
-        cudaError_t e;
-        if (h->esz == 8) {
-            double* fp[3] = {(double*)h->state[h->cur][0], (double*)h->state[h->cur][1], (double*)h->state[h->cur][2]};
-            e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, +1, h->stream);
-        } else {
-            float* fp[3] = {(float*)h->state[h->cur][0], (float*)h->state[h->cur][1], (float*)h->state[h->cur][2]};
-            e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, +1, h->stream);
-        }
-        CK(h, e);
-        h->launches++;
-    }
+    int rc = frame_change(h, h->state[h->cur], +1);
+    if (rc) return rc;
     CK(h, cudaStreamSynchronize(h->stream));
     return BT_OK;
 }
@@ -451,65 +610,33 @@ int bt_set_state(bt_handle* h, const double* mx, const double* my, const double*
 int bt_set_state_device(bt_handle* h, const void* mx, const void* my, const void* mz) {
     if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    const bt_config& c = h->cfg;
     const void* src[3] = {mx, my, mz};
     for (int a = 0; a < 3; ++a)
-        CK(h, cudaMemcpyAsync(h->state[h->cur][a], src[a], h->esz * h->nvox, cudaMemcpyDeviceToDevice, h->stream));
-    double k[3];
-    kvec_at(h, h->step, k);
-    if (k[0] != 0.0 || k[1] != 0.0 || k[2] != 0.0) {
-        const bt_config& c = h->cfg;
-        cudaError_t e;
-        if (h->esz == 8) {
-            double* fp[3] = {(double*)h->state[h->cur][0], (double*)h->state[h->cur][1], (double*)h->state[h->cur][2]};
-            e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, +1, h->stream);
-        } else {
-            float* fp[3] = {(float*)h->state[h->cur][0], (float*)h->state[h->cur][1], (float*)h->state[h->cur][2]};
-            e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, +1, h->stream);
-        }
-        CK(h, e);
-        h->launches++;
-    }
-    return BT_OK;
+        CK(h, cudaMemcpy2DAsync(h->state[h->cur][a], h->pitch * h->esz, src[a], c.nx * h->esz, c.nx * h->esz,
+                                (size_t)c.ny * c.nz, cudaMemcpyDeviceToDevice, h->stream));
+    return frame_change(h, h->state[h->cur], +1);
 }
 
 int bt_get_state(bt_handle* h, double* mx, double* my, double* mz) {
     if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
-    const bt_config& c = h->cfg;
     double k[3];
     kvec_at(h, h->step, k);
     const bool phase = (k[0] != 0.0 || k[1] != 0.0 || k[2] != 0.0);
-    // the idle ping-pong buffer holds the lab-frame copy
+    // the idle ping-pong buffer holds the lab-frame copy; the next step overwrites it
     void** src = h->state[h->cur];
     void** tmp = h->state[1 - h->cur];
     if (phase) {
         for (int a = 0; a < 2; ++a)
-            CK(h, cudaMemcpyAsync(tmp[a], src[a], h->esz * h->nvox, cudaMemcpyDeviceToDevice, h->stream));
-        cudaError_t e;
-        if (h->esz == 8) {
-            double* fp[3] = {(double*)tmp[0], (double*)tmp[1], (double*)tmp[2]};
-            e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, -1, h->stream);
-        } else {
-            float* fp[3] = {(float*)tmp[0], (float*)tmp[1], (float*)tmp[2]};
-            e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, k[0], k[1], k[2], c.dx, c.dy, c.dz, -1, h->stream);
-        }
-        CK(h, e);
-        h->launches++;
+            CK(h, cudaMemcpyAsync(tmp[a], src[a], h->esz * h->comp, cudaMemcpyDeviceToDevice, h->stream));
+        int rc = frame_change(h, tmp, -1);
+        if (rc) return rc;
     }
     double* dst[3] = {mx, my, mz};
-    std::vector<float> f;
-    if (h->esz == 4) f.resize(h->nvox);
     for (int a = 0; a < 3; ++a) {
-        const void* s = (phase && a < 2) ? tmp[a] : src[a];
-        if (h->esz == 8) {
-            CK(h, cudaMemcpyAsync(dst[a], s, 8 * h->nvox, cudaMemcpyDeviceToHost, h->stream));
-            CK(h, cudaStreamSynchronize(h->stream));
-        } else {
-            CK(h, cudaMemcpyAsync(f.data(), s, 4 * h->nvox, cudaMemcpyDeviceToHost, h->stream));
-            CK(h, cudaStreamSynchronize(h->stream));
-            for (size_t q = 0; q < h->nvox; ++q) dst[a][q] = (double)f[q];
-        }
+        int rc = get_component(h, dst[a], (phase && a < 2) ? tmp[a] : src[a]);
+        if (rc) return rc;
     }
-    // the idle buffer is garbage now; the next step overwrites all of it
     return BT_OK;
 }
 
@@ -544,38 +671,44 @@ int bt_run_async(bt_handle* h, long long nsteps) {
     int rc = ensure_mt(h, nsteps);
     if (rc) return rc;
     // ctl: step and mt_base for this run (written in stream order)
+    CK(h, cudaStreamSynchronize(h->stream));
     h->ctl_h->step = h->step;
     h->ctl_h->mt_base = h->step;
     h->ctl_h->ticket = 0;
     h->ctl_h->status = 0;
     CK(h, cudaMemcpyAsync(h->ctl_d, h->ctl_h, sizeof(bt::Ctl), cudaMemcpyHostToDevice, h->stream));
-    long long left = nsteps;
-    // whole graphs of GRAPH_STEPS launches, then single launches
-    while (left >= GRAPH_STEPS) {
-        cudaGraphExec_t& g = h->graph[h->cur];
-        if (!g) {
-            cudaGraph_t graph;
-            CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-            cudaError_t e = cudaSuccess;
-            const long long before = h->launches;
-            for (int q = 0; q < GRAPH_STEPS && e == cudaSuccess; ++q) e = launch_one(h, (h->cur + q) & 1);
-            h->launches = before;
-            cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
-            CK(h, e);
-            CK(h, e2);
-            e = cudaGraphInstantiate(&g, graph, 0);
-            cudaGraphDestroy(graph);
-            CK(h, e);
+    long long s = h->step;
+    const long long end = h->step + nsteps;
+    while (s < end) {
+        bool clean = end - s >= GRAPH_STEPS;
+        for (long long q = s; clean && q < s + GRAPH_STEPS; ++q) clean = !step_has_pulse(h, q);
+        if (clean) {
+            // a graph of GRAPH_STEPS pulse-free launches, captured once per input side
+            cudaGraphExec_t& g = h->graph[h->cur];
+            if (!g) {
+                cudaGraph_t graph;
+                CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+                cudaError_t e = cudaSuccess;
+                const long long before = h->launches;
+                for (int q = 0; q < GRAPH_STEPS && e == cudaSuccess; ++q) e = launch_one(h, (h->cur + q) & 1, s + q);
+                h->launches = before;
+                cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+                CK(h, e);
+                CK(h, e2);
+                e = cudaGraphInstantiate(&g, graph, 0);
+                cudaGraphDestroy(graph);
+                CK(h, e);
+            }
+            CK(h, cudaGraphLaunch(g, h->stream));
+            h->launches += GRAPH_STEPS;
+            s += GRAPH_STEPS;
+        } else {
+            CK(h, launch_one(h, h->cur, s));
+            h->cur ^= 1;
+            s += 1;
         }
-        CK(h, cudaGraphLaunch(g, h->stream));
-        h->launches += GRAPH_STEPS;
-        left -= GRAPH_STEPS;
     }
-    for (long long q = 0; q < left; ++q) {
-        CK(h, launch_one(h, h->cur));
-        h->cur ^= 1;
-    }
-    h->step += nsteps;
+    h->step = end;
     h->last_run = nsteps;
     return BT_OK;
 }
@@ -625,5 +758,69 @@ int bt_measure(bt_handle* h, double* sums3) {
 }
 
 long long bt_launch_count(const bt_handle* h) { return h ? h->launches : -1; }
+
+int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
+    if (!h || trial_steps <= 0) return fail(h, BT_E_ARG, "bad autotune arguments");
+    if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    if (h->cfg.precision != BT_F32 || !h->use_tma) {
+        if (best_zsplit) *best_zsplit = (int)h->grid.z;
+        return BT_OK;
+    }
+    // candidate z-splits: waves of 2 CTAs per SM from 1 to 8, chunks of >= 4 planes
+    const bt_config& c = h->cfg;
+    const long long tiles = (long long)h->tgrid.y * h->tgrid.z;
+    std::vector<int> cand;
+    for (int waves = 1; waves <= 8; ++waves) {
+        const long long zs = (waves * 2LL * h->num_sms + tiles - 1) / tiles;
+        if (zs >= 1 && zs <= std::max(1, c.nz / 4)) cand.push_back((int)zs);
+    }
+    cand.push_back(default_tma_split(h));
+    std::sort(cand.begin(), cand.end());
+    cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+    // the trial runs advance the field; the caller's field and step are restored
+    const long long step0 = h->step;
+    const int cur0 = h->cur;
+    void* keep = nullptr;
+    const size_t sbytes = 3 * h->esz * h->comp;
+    CK(h, cudaMalloc(&keep, sbytes));
+    CK(h, cudaMemcpyAsync(keep, h->state_base[h->cur], sbytes, cudaMemcpyDeviceToDevice, h->stream));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int best_zs = (int)h->tgrid.x;
+    int rc = BT_OK;
+    for (int& zs : cand) zs = normalise_split(c.nz, zs);
+    std::sort(cand.begin(), cand.end());
+    cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+    for (int zs : cand) {
+        if ((rc = set_tma_split(h, zs))) break;
+        if ((rc = bt_run_async(h, GRAPH_STEPS))) break;  // warm-up and graph capture
+        cudaEventRecord(e0, h->stream);
+        if ((rc = bt_run_async(h, trial_steps))) break;
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if ((rc = check_ctl(h))) break;
+        if (ms < best) {
+            best = ms;
+            best_zs = zs;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamSynchronize(h->stream);
+    h->cur = cur0;
+    cudaMemcpy(h->state_base[h->cur], keep, sbytes, cudaMemcpyDeviceToDevice);
+    cudaFree(keep);
+    if (rc) return rc;
+    rc = set_tma_split(h, best_zs);
+    if (rc) return rc;
+    rc = bt_set_step(h, step0);
+    if (rc) return rc;
+    if (best_zsplit) *best_zsplit = best_zs;
+    return BT_OK;
+}
 
 }  // extern "C"

@@ -1,6 +1,7 @@
 // Internal types shared by the step kernels and the host runtime.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace bt {
@@ -45,16 +46,22 @@ struct Ctl {
     int status;          // 0 ok, 1 = M(t) buffer overflow, 2 = schedule missing
 };
 
+// Device layouts are pitched so that every row starts on a 16-byte boundary
+// (a TMA requirement): the state, vy and vz use row pitch `pitch` (nx rounded
+// up to 4 elements), vx uses `vxpitch` (nx+1 rounded up to 4), the geometry
+// code `cpitch` (nx rounded up to 16). Padding columns are never read as data.
 template <typename T>
 struct StepParams {
     int nx, ny, nz, zchunk;
-    long long plane;            // nx * ny
+    int pitch, vxpitch, cpitch;
+    int zsplit;
+    long long plane;            // pitch * ny (state and vz plane stride)
     const T* in[3];
     T* out[3];
-    const uint8_t* code;
-    const T* vx;                // [nz][ny][nx+1]
-    const T* vy;                // [nz][ny+1][nx]
-    const T* vz;                // [nz+1][ny][nx]
+    const uint8_t* code;        // [nz][ny][cpitch]
+    const T* vx;                // [nz][ny][vxpitch], faces 0..nx
+    const T* vy;                // [nz][ny+1][pitch], faces 0..ny
+    const T* vz;                // [nz+1][ny][pitch], faces 0..nz
     // reference update constants, formed on the host in FP64 in the
     // reference's operation order, then rounded to T
     T hx, hy, hz, hxx, hyy, hzz;
@@ -76,13 +83,25 @@ struct StepParams {
     long long mt_cap;
 };
 
+// TMA descriptors of the FP32 fast path (one per ping-pong input side)
+struct TmaMaps {
+    CUtensorMap state;   // 4D {x, y, z, component} over the input field
+    CUtensorMap vx, vy, vz, code;
+};
+
 // launchers (bt_step_f32.cu / bt_step_f64.cu)
 template <typename T>
 cudaError_t launch_step(const StepParams<T>& p, int scheme, int vel, int prec, dim3 grid, cudaStream_t s);
 template <typename T>
 cudaError_t launch_sums(const StepParams<T>& p, double* out4, cudaStream_t s);
+// FP32 fast path: TMA-staged plane tiles, 4 voxels per thread, no pulses
+cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
+                            cudaStream_t s);
+int tma_smem_bytes();
+constexpr int TMA_TX = 128;  // tile width (voxels along x) of the fast path
+constexpr int TMA_TY = 8;    // tile height (rows along y) of the fast path
 template <typename T>
-cudaError_t launch_frame(T* f[3], const uint8_t* code, int nx, int ny, int nz, double kx, double ky,
-                         double kz, double dx, double dy, double dz, int sign, cudaStream_t s);
+cudaError_t launch_frame(T* f[3], const uint8_t* code, int nx, int ny, int nz, int pitch, int cpitch, double kx,
+                         double ky, double kz, double dx, double dy, double dz, int sign, cudaStream_t s);
 
 }  // namespace bt

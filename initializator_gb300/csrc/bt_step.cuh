@@ -83,17 +83,20 @@ __device__ __forceinline__ void apply_pulse(const DevPulse& pu, double& mx, doub
         ort(mx, my, mz, ax, ay, az, angle);
     } else if (pu.flag == 3) {
         const double distance = 10e+12;
-        angle = g * pu.eff *
-                pow(pow(((double)(x + 1) - 1.0 - distance) * dx * pu.naxis[0] +
-                            ((double)(y + 1) - 1.0 - distance) * dy * pu.naxis[1] +
-                            ((double)(z + 1) - 1.0 - distance) * dz * pu.naxis[2],
-                        2),
-                    0.5);
+        // pow(pow(X, 2), 0.5) of the reference; glibc's pow returns exactly
+        // X*X for exponent 2 and sqrt(Y) for exponent 0.5, which the device
+        // reproduces with the correctly rounded forms (the angle is ~1e6 rad,
+        // so one ulp of it would move the field by ~1e-10)
+        const double X = ((double)(x + 1) - 1.0 - distance) * dx * pu.naxis[0] +
+                         ((double)(y + 1) - 1.0 - distance) * dy * pu.naxis[1] +
+                         ((double)(z + 1) - 1.0 - distance) * dz * pu.naxis[2];
+        angle = g * pu.eff * sqrt(X * X);
         ort(mx, my, mz, pu.naxis[0], pu.naxis[1], pu.naxis[2], angle);
     } else if (pu.flag == 4) {
-        angle = 0.0 - g * sqrt(pow(((double)(x + 1) - 0.5) * dx * ax - 0.5 * nx * dx * ax, 2.0) +
-                               pow(((double)(y + 1) - 0.5) * dy * ay - 0.5 * ny * dy * ay, 2.0) +
-                               pow(((double)(z + 1) - 0.5) * dz * az - 0.5 * nz * dz * az, 2.0));
+        const double a = ((double)(x + 1) - 0.5) * dx * ax - 0.5 * nx * dx * ax;
+        const double b = ((double)(y + 1) - 0.5) * dy * ay - 0.5 * ny * dy * ay;
+        const double c = ((double)(z + 1) - 0.5) * dz * az - 0.5 * nz * dz * az;
+        angle = 0.0 - g * sqrt(a * a + b * b + c * c);
         ort(mx, my, mz, ax, ay, az, angle);
     }
 }
@@ -137,11 +140,14 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
     const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched);
     const bool inb = (x < nx) && (y < ny);
     const int xc = min(x, nx - 1), yc = min(y, ny - 1);
+    const int pitch = P.pitch;
     const long long plane = P.plane;
-    const long long col = (long long)yc * nx + xc;
-    const long long vxrow = (long long)yc * (nx + 1) + xc;
-    const long long vxplane = (long long)ny * (nx + 1);
-    const long long vyplane = (long long)(ny + 1) * nx;
+    const long long col = (long long)yc * pitch + xc;
+    const long long ccol = (long long)yc * P.cpitch + xc;
+    const long long cplane = (long long)P.cpitch * ny;
+    const long long vxrow = (long long)yc * P.vxpitch + xc;
+    const long long vxplane = (long long)ny * P.vxpitch;
+    const long long vyplane = (long long)(ny + 1) * pitch;
 
     // per-step uniform values
     T gdx = 0, gdy = 0, gdz = 0;
@@ -172,9 +178,12 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
     // rolling column
     T cb[3], cc[3], ca[3];
     {
-        const long long ob = (long long)max(z0 - 1, 0) * plane + col;
-        const long long oc = (long long)z0 * plane + col;
-        const long long oa = (long long)min(z0 + 1, nz - 1) * plane + col;
+        // clamped so that a CTA with an empty chunk (z0 >= nz; the host never
+        // makes one) still reads inside the field
+        const int zb = min(max(z0 - 1, 0), nz - 1), zcur = min(z0, nz - 1), za = min(z0 + 1, nz - 1);
+        const long long ob = (long long)zb * plane + col;
+        const long long oc = (long long)zcur * plane + col;
+        const long long oa = (long long)za * plane + col;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             cb[c] = P.in[c][ob];
@@ -183,7 +192,7 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
         }
     }
     T wlo = 0;
-    if constexpr (VEL) wlo = P.vz[(long long)z0 * plane + col];
+    if constexpr (VEL) wlo = P.vz[(long long)min(z0, nz - 1) * plane + col];
 
     for (int z = z0; z < z1; ++z) {
         // prefetch the plane after next for the rolling column
@@ -192,35 +201,35 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
 #pragma unroll
         for (int c = 0; c < 3; ++c) nxt[c] = P.in[c][on];
         const long long oz = (long long)z * plane;
-        const uint8_t cd = P.code[oz + col];
+        const uint8_t cd = P.code[(long long)z * cplane + ccol];
         T um = 0, up = 0, vm = 0, vp = 0, whi = 0;
         if constexpr (VEL) {
             um = P.vx[(long long)z * vxplane + vxrow];
             up = P.vx[(long long)z * vxplane + vxrow + 1];
             vm = P.vy[(long long)z * vyplane + col];
-            vp = P.vy[(long long)z * vyplane + col + nx];
+            vp = P.vy[(long long)z * vyplane + col + pitch];
             whi = P.vz[(long long)(z + 1) * plane + col];
         }
         __syncthreads();
 #pragma unroll
         for (int c = 0; c < 3; ++c) sm[c][ty + 1][tx + 1] = cc[c];
         if (tx == 0) {
-            const long long o = oz + (long long)yc * nx + max(x - 1, 0);
+            const long long o = oz + (long long)yc * pitch + max(x - 1, 0);
 #pragma unroll
             for (int c = 0; c < 3; ++c) sm[c][ty + 1][0] = P.in[c][o];
         }
         if (tx == TX - 1) {
-            const long long o = oz + (long long)yc * nx + min(x + 1, nx - 1);
+            const long long o = oz + (long long)yc * pitch + min(x + 1, nx - 1);
 #pragma unroll
             for (int c = 0; c < 3; ++c) sm[c][ty + 1][TX + 1] = P.in[c][o];
         }
         if (ty == 0) {
-            const long long o = oz + (long long)max(y - 1, 0) * nx + xc;
+            const long long o = oz + (long long)max(y - 1, 0) * pitch + xc;
 #pragma unroll
             for (int c = 0; c < 3; ++c) sm[c][0][tx + 1] = P.in[c][o];
         }
         if (ty == TY - 1) {
-            const long long o = oz + (long long)min(y + 1, ny - 1) * nx + xc;
+            const long long o = oz + (long long)min(y + 1, ny - 1) * pitch + xc;
 #pragma unroll
             for (int c = 0; c < 3; ++c) sm[c][TY + 1][tx + 1] = P.in[c][o];
         }
@@ -422,11 +431,12 @@ __global__ void sums_kernel(const __grid_constant__ StepParams<T> P, double kx, 
     __shared__ double red[NTHREADS / 32][4];
     const int tid = threadIdx.x;
     double s[4] = {0.0, 0.0, 0.0, 0.0};
-    const long long n = P.plane * P.nz;
+    const long long n = (long long)P.nx * P.ny * P.nz;
     const bool phase = (kx != 0.0 || ky != 0.0 || kz != 0.0);
-    for (long long q = blockIdx.x * (long long)NTHREADS + tid; q < n; q += (long long)gridDim.x * NTHREADS) {
-        if (!(P.code[q] & CODE_PORE)) continue;
-        const int x = (int)(q % P.nx), y = (int)((q / P.nx) % P.ny), z = (int)(q / P.plane);
+    for (long long qq = blockIdx.x * (long long)NTHREADS + tid; qq < n; qq += (long long)gridDim.x * NTHREADS) {
+        const int x = (int)(qq % P.nx), y = (int)((qq / P.nx) % P.ny), z = (int)(qq / ((long long)P.nx * P.ny));
+        if (!(P.code[((long long)z * P.ny + y) * P.cpitch + x] & CODE_PORE)) continue;
+        const long long q = ((long long)z * P.ny + y) * P.pitch + x;
         if (x < P.box[0] || x >= P.box[1] || y < P.box[2] || y >= P.box[3] || z < P.box[4] || z >= P.box[5]) continue;
         double a = (double)P.in[0][q], b = (double)P.in[1][q];
         if (phase) {
@@ -462,13 +472,14 @@ __global__ void sums_kernel(const __grid_constant__ StepParams<T> P, double kx, 
 
 // frame change of the transverse field: (f0 + i f1) *= exp(sign * i * k.r)
 template <typename T>
-__global__ void frame_kernel(T* f0, T* f1, const uint8_t* code, int nx, int ny, int nz, double kx, double ky,
-                             double kz, double dx, double dy, double dz, int sign) {
+__global__ void frame_kernel(T* f0, T* f1, const uint8_t* code, int nx, int ny, int nz, int pitch, int cpitch,
+                             double kx, double ky, double kz, double dx, double dy, double dz, int sign) {
     const long long n = (long long)nx * ny * nz;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-         q += (long long)gridDim.x * blockDim.x) {
-        if (!(code[q] & CODE_PORE)) continue;
-        const int x = (int)(q % nx), y = (int)((q / nx) % ny), z = (int)(q / ((long long)nx * ny));
+    for (long long qq = blockIdx.x * (long long)blockDim.x + threadIdx.x; qq < n;
+         qq += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(qq % nx), y = (int)((qq / nx) % ny), z = (int)(qq / ((long long)nx * ny));
+        if (!(code[((long long)z * ny + y) * cpitch + x] & CODE_PORE)) continue;
+        const long long q = ((long long)z * ny + y) * pitch + x;
         const double ang = sign * (kx * ((x + 0.5) * dx) + ky * ((y + 0.5) * dy) + kz * ((z + 0.5) * dz));
         double sn, cs;
         sincos(ang, &sn, &cs);

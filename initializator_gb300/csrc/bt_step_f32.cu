@@ -1,6 +1,6 @@
 // float instantiation of the fused step kernel and its helpers.
 // Compiled with the default -fmad=true (FP32 production path).
-#include "bt_step.cuh"
+#include "bt_step_tma.cuh"
 
 namespace bt {
 
@@ -18,10 +18,38 @@ cudaError_t launch_sums<float>(const StepParams<float>& p, double* kvec_and_grid
 }
 
 template <>
-cudaError_t launch_frame<float>(float* f[3], const uint8_t* code, int nx, int ny, int nz, double kx, double ky,
-                                double kz, double dx, double dy, double dz, int sign, cudaStream_t s) {
-    frame_kernel<float><<<1216, 256, 0, s>>>(f[0], f[1], code, nx, ny, nz, kx, ky, kz, dx, dy, dz, sign);
+cudaError_t launch_frame<float>(float* f[3], const uint8_t* code, int nx, int ny, int nz, int pitch, int cpitch,
+                                double kx, double ky, double kz, double dx, double dy, double dz, int sign,
+                                cudaStream_t s) {
+    frame_kernel<float><<<1216, 256, 0, s>>>(f[0], f[1], code, nx, ny, nz, pitch, cpitch, kx, ky, kz, dx, dy, dz, sign);
     return cudaGetLastError();
+}
+
+int tma_smem_bytes() { return tma::SMEM; }
+
+template <int SCHEME, bool VEL, bool PREC>
+static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, tma::SMEM);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    step_tma_kernel<SCHEME, VEL, PREC><<<grid, tma::NT, tma::SMEM, s>>>(p, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
+                            cudaStream_t s) {
+    if (scheme == SCHEME_REF) {
+        if (vel && prec) return launch_tma_t<SCHEME_REF, true, true>(p, m, grid, s);
+        if (vel) return launch_tma_t<SCHEME_REF, true, false>(p, m, grid, s);
+        if (prec) return launch_tma_t<SCHEME_REF, false, true>(p, m, grid, s);
+        return launch_tma_t<SCHEME_REF, false, false>(p, m, grid, s);
+    }
+    if (vel) return launch_tma_t<SCHEME_KSPACE, true, false>(p, m, grid, s);
+    return launch_tma_t<SCHEME_KSPACE, false, false>(p, m, grid, s);
 }
 
 }  // namespace bt

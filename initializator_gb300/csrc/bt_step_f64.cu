@@ -19,9 +19,10 @@ cudaError_t launch_sums<double>(const StepParams<double>& p, double* kvec_and_gr
 }
 
 template <>
-cudaError_t launch_frame<double>(double* f[3], const uint8_t* code, int nx, int ny, int nz, double kx, double ky,
-                                double kz, double dx, double dy, double dz, int sign, cudaStream_t s) {
-    frame_kernel<double><<<1216, 256, 0, s>>>(f[0], f[1], code, nx, ny, nz, kx, ky, kz, dx, dy, dz, sign);
+cudaError_t launch_frame<double>(double* f[3], const uint8_t* code, int nx, int ny, int nz, int pitch, int cpitch,
+                                double kx, double ky, double kz, double dx, double dy, double dz, int sign,
+                                cudaStream_t s) {
+    frame_kernel<double><<<1216, 256, 0, s>>>(f[0], f[1], code, nx, ny, nz, pitch, cpitch, kx, ky, kz, dx, dy, dz, sign);
     return cudaGetLastError();
 }
 

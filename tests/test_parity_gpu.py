@@ -66,7 +66,8 @@ def _random_case(shape, seed, flow=True, prec=True):
     st0 = rng.uniform(-1, 1, (3,) + shape) * mask
     kw = dict(dx=1e-6, dy=1.1e-6, dz=0.9e-6, dt=geometry.stable_dt(1.1e-6, 2.3e-9) * 0.8, main_field=(0.2, 0.3, 0.9),
               grad=(0.02, -0.03, 0.05), d_pore=2.3e-9, t1=0.1, t2=0.05, rho1=3e-5, rho2=5e-5, p_eq=0.5,
-              vector_mult=1 if prec else 0, velocity=1 if flow else 0, diffusion=1, buffer=(1, 2, 0))
+              vector_mult=1 if prec else 0, velocity=1 if flow else 0, diffusion=1,
+              buffer=(min(1, shape[2] // 2), min(2, shape[1] // 2), 0))
     return mask, vel, st0, kw
 
 
@@ -214,3 +215,59 @@ def test_conservation_256(btlib):
         s.set_state(st0)
         mt = s.run(100)
     assert abs(mt[-1, 0] / mask.sum() - 1.0) < 1e-5
+
+
+@pytest.mark.parametrize("shape", [(33, 9, 65), (8, 16, 130), (5, 17, 257), (70, 3, 4)])
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_tma_path_matches_generic(shape, scheme, btlib, monkeypatch):
+    """The FP32 TMA fast path (pulse-free steps) against the generic FP32 kernel:
+    same update, different FP32 operation order -> fields within 1e-5."""
+    import initializator_gb300 as bt
+    mask, vel, st0, kw = _random_case(shape, seed=11 + sum(shape))
+    if scheme == bt.BT_SCHEME_KSPACE:
+        kw.update(main_field=(0, 0, 1), vector_mult=0, gamma=bt.GAMMA_PROTON)
+        wave = bt.kspace_waveform_pgse(80, kw["dt"], 0.05, 8 * kw["dt"], 40 * kw["dt"], axis=(0.2, 0.5, 1.0))
+    outs = []
+    for no_tma in ("1", None):
+        if no_tma:
+            monkeypatch.setenv("BT_NO_TMA", no_tma)
+        else:
+            monkeypatch.delenv("BT_NO_TMA", raising=False)
+        with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, scheme=scheme, **kw)) as s:
+            s.upload_geometry(mask, vel)
+            if scheme == bt.BT_SCHEME_KSPACE:
+                s.set_schedule([], grad_wave=wave)
+            s.set_state(st0)
+            mt = s.run(80)
+            outs.append((s.get_state(), mt))
+    assert rel_err(outs[1][0], outs[0][0]) <= 1e-5
+    assert rel_err(outs[1][1], outs[0][1]) <= 1e-5
+
+
+def test_tma_zsplits_and_autotune(btlib, monkeypatch):
+    """Any z-chunking of the fast path gives the same field (chunks never come
+    out empty: 38 chunks of 256 planes would leave the last one empty without
+    the host's normalisation), and the autotuner restores field and step."""
+    import initializator_gb300 as bt
+    shape = (256, 8, 128)
+    mask, vel, st0, kw = _random_case(shape, seed=3)
+    fields = []
+    for zs in ("1", "5", "38", "200"):
+        monkeypatch.setenv("BT_TMA_ZSPLIT", zs)
+        with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, **kw)) as s:
+            s.upload_geometry(mask, vel)
+            s.set_state(st0)
+            mt = s.run(40)
+            fields.append((s.get_state(), mt))
+    for st, mt in fields[1:]:
+        assert np.array_equal(st, fields[0][0])
+        assert rel_err(mt, fields[0][1]) <= 1e-6
+    monkeypatch.delenv("BT_TMA_ZSPLIT")
+    with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, **kw)) as s:
+        s.upload_geometry(mask, vel)
+        s.set_state(st0)
+        best = s.autotune(8)
+        assert best >= 1 and s.step == 0
+        assert rel_err(s.get_state(), st0) <= 1e-7
+        s.run(40)
+        assert np.array_equal(s.get_state(), fields[0][0])
