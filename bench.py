@@ -217,13 +217,16 @@ def run_ours(args):
     mask, vel = build_workload(f"cuda:{lr}", seed=SEED + r)
     kw, wave, rf = physics(total)
     nvox = int(np.prod(SHAPE))
+    if args.zsplit:
+        os.environ["BT_TMA_ZSPLIT"] = str(args.zsplit)
     s = bt.Solver(bt.make_config(SHAPE, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, **kw))
     s.upload_geometry(mask, vel)
     s.set_schedule(rf, grad_wave=wave)
     st0 = np.zeros((3,) + SHAPE)
     st0[0] = mask
     s.set_state(st0)
-    zsplit = s.autotune(64)  # picks the z-chunking of the fast path; restores field and step
+    # the autotuner picks the z-chunking of the fast path (field and step restored)
+    zsplit = args.zsplit if args.zsplit else s.autotune(64)
     stream = torch.cuda.ExternalStream(s.stream_ptr)
 
     def barrier():
@@ -324,6 +327,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--zsplit", type=int, default=0, help="fixed z-chunking of the fast path (skips the autotuner)")
     ap.add_argument("--profile", action="store_true",
                     help="device-resident phase only (for ncu captures); prints no bench line")
     args = ap.parse_args()

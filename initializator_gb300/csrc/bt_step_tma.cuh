@@ -47,7 +47,7 @@ constexpr int OFF_CODE = OFF_VZ + SZ_VZ;                    // 29312
 constexpr int SZ_CODE = TH * TW;                            // 1024
 constexpr int STAGE = OFF_CODE + SZ_CODE;                   // 30336
 constexpr int OFF_AUX = NSTAGE * STAGE;                     // tables, barriers, reduction
-constexpr int SMEM = OFF_AUX + 2048 + 8 * ZCHUNK_MAX + 128;  // + 128 for the base alignment
+constexpr int SMEM = OFF_AUX + 4608 + 8 * ZCHUNK_MAX + 128;  // + 128 for the base alignment
 static_assert(OFF_VX % 128 == 0 && OFF_VY % 128 == 0 && OFF_VZ % 128 == 0 && OFF_CODE % 128 == 0, "align");
 static_assert(STAGE % 128 == 0, "align");
 constexpr uint32_t WAIT_LIMIT = 1u << 20;  // polls; a healthy copy lands in microseconds
@@ -106,29 +106,30 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // shared-memory base explicitly (the launch reserves 128 spare bytes)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem = smem_raw + ((128u - (sa(smem_raw) & 127u)) & 127u);
-    float* s_dtt1 = reinterpret_cast<float*>(smem + OFF_AUX);           // 64
-    float* s_dtt2 = s_dtt1 + 64;                                        // 64
-    float2* s_ex = reinterpret_cast<float2*>(s_dtt2 + 64);              // TW
-    float2* s_ey = s_ex + TW;                                           // TH
-    // aux layout (bytes from OFF_AUX): dtt1 0..255, dtt2 256..511, ex 512..1535,
-    // ey 1536..1599, barriers 1600..1623, flags 1664..1671, red 1728..1919, ez 2048..
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_AUX + 1600);  // NSTAGE
-    int* s_flags = reinterpret_cast<int*>(smem + OFF_AUX + 1664);       // abort, last
-    double* red = reinterpret_cast<double*>(smem + OFF_AUX + 1728);     // [TH][3]
-    float2* s_ez = reinterpret_cast<float2*>(smem + OFF_AUX + 2048);    // ZCHUNK_MAX
+    // aux layout (bytes from OFF_AUX): code table 0..4095 (128 rows x 8 floats),
+    // ey 4096..4159, barriers 4160..4183, flags 4224..4231, red 4288..4479, ez 4608..
+    float4* s_tab = reinterpret_cast<float4*>(smem + OFF_AUX);
+    float2* s_ey = reinterpret_cast<float2*>(smem + OFF_AUX + 4096);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_AUX + 4160);
+    int* s_flags = reinterpret_cast<int*>(smem + OFF_AUX + 4224);
+    double* red = reinterpret_cast<double*>(smem + OFF_AUX + 4288);
+    float2* s_ez = reinterpret_cast<float2*>(smem + OFF_AUX + 4608);
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, w = tid >> 5;
     const int nx = P.nx, ny = P.ny, nz = P.nz;
-    // blockIdx.x walks the z-chunks of one tile, so neighbouring chunks (which
-    // share their boundary planes) run side by side and meet in L2
+    // blockIdx.x walks the z-chunks of one tile. Odd chunks march downwards,
+    // so the plane two neighbouring chunks share is read by both at the same
+    // moment (both at their start, or both at their end) and the second read
+    // hits L2 instead of DRAM.
     const int zc = blockIdx.x;
     const int x0 = blockIdx.y * TW, y0 = blockIdx.z * TH;
     const int z0 = zc * P.zchunk;
     const int z1 = min(nz, z0 + P.zchunk);
+    const int d = (zc & 1) ? -1 : 1;
     const long long step = __ldcg(&P.ctl->step);
     const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched);
-    const int xb = x0 + QX * lane;        // first of this thread's 4 voxels
+    const int xb = x0 + QX * lane;  // first of this thread's 4 voxels
     const int y = y0 + w;
 
     uint32_t txbytes = SZ_STATE + SZ_CODE;
@@ -145,28 +146,42 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
         tma_load_3d(base + OFF_CODE, &M.code, bar, x0, y0, plane);
     };
+    // plane sequence: q = 0 is the ghost-side plane, then the chunk in marching order
+    auto plane_of = [&](int q) { return d > 0 ? z0 - 1 + q : z1 - q; };
     // the host never makes an empty chunk; a CTA that still gets one issues
     // no copy, waits on nothing and contributes zero sums
     const bool empty = z1 <= z0;
-    const int nplanes = empty ? 0 : z1 - z0 + 2;  // z0-1 .. z1
-    int issued[NSTAGE] = {0, 0, 0};              // copies issued per slot (thread 0)
+    const int nplanes = empty ? 0 : z1 - z0 + 2;
+    // plane q lands in slot q % NSTAGE as that slot's (q / NSTAGE)-th phase
+    int n_issued = 0;  // planes issued so far (thread 0), always in plane order
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
         s_flags[0] = 0;
         for (int q = 0; q < NSTAGE && q < nplanes; ++q) {
-            issue(q, z0 - 1 + q);
-            issued[q]++;
+            issue(q, plane_of(q));
+            n_issued++;
         }
     }
-    // per-CTA tables
-    if (tid < 64) {
-        s_dtt1[tid] = P.dtt1[tid];
-        s_dtt2[tid] = P.dtt2[tid];
+    // per-CTA table indexed by the voxel code (bit 6 pore, bits 0-5 solid
+    // faces): six face diffusion weights, dt/T1, dt/T2; all zero for solid
+    if (tid < 128) {
+        const int f = tid & 63;
+        const bool pore = tid & 64;
+        const float dm = (pore && P.diffusion) ? 1.f : 0.f;
+        const float kx = P.hxx * P.dpp, ky = P.hyy * P.dpp, kz = P.hzz * P.dpp;
+        const float sx = P.hxx * P.dps, sy = P.hyy * P.dps, sz = P.hzz * P.dps;
+        s_tab[2 * tid] = make_float4(dm * ((f & 1) ? sx : kx), dm * ((f & 2) ? sx : kx), dm * ((f & 4) ? sy : ky),
+                                     dm * ((f & 8) ? sy : ky));
+        s_tab[2 * tid + 1] = make_float4(dm * ((f & 16) ? sz : kz), dm * ((f & 32) ? sz : kz),
+                                         pore ? P.dtt1[f] : 0.f, pore ? P.dtt2[f] : 0.f);
     }
+    // lab-frame phase of this thread's 4 columns (KSPACE), FP64-reduced arguments
+    float exr[QX] = {1.f, 1.f, 1.f, 1.f}, exi[QX] = {0.f, 0.f, 0.f, 0.f};
     if constexpr (SCHEME == SCHEME_KSPACE) {
-        if (tid < TW) lab_phase<float>(si->knext[0], x0 + tid, P.dxd, s_ex[tid].x, s_ex[tid].y);
-        if (tid >= TW && tid < TW + TH) lab_phase<float>(si->knext[1], y0 + tid - TW, P.dyd, s_ey[tid - TW].x, s_ey[tid - TW].y);
+#pragma unroll
+        for (int i = 0; i < QX; ++i) lab_phase<float>(si->knext[0], xb + i, P.dxd, exr[i], exi[i]);
+        if (tid < TH) lab_phase<float>(si->knext[1], y0 + tid, P.dyd, s_ey[tid].x, s_ey[tid].y);
         for (int q = tid; q < z1 - z0; q += NT) lab_phase<float>(si->knext[2], z0 + q, P.dzd, s_ez[q].x, s_ez[q].y);
     }
     __syncthreads();
@@ -178,24 +193,29 @@ __global__ void __launch_bounds__(tma::NT, 2)
         gdy = (float)(si->grad[1] * P.dyd);
         gdz = (float)(si->grad[2] * P.dzd);
     }
-    float ph[6][2];
+    float ph[3][2];  // exp(+i k d) per axis; the + face uses its conjugate
     if constexpr (SCHEME == SCHEME_KSPACE) {
 #pragma unroll
-        for (int f = 0; f < 6; ++f) {
-            ph[f][0] = (float)si->phase[f][0];
-            ph[f][1] = (float)si->phase[f][1];
+        for (int a = 0; a < 3; ++a) {
+            ph[a][0] = (float)si->phase[2 * a][0];
+            ph[a][1] = (float)si->phase[2 * a][1];
         }
     }
-    const float kpp_x = P.hxx * P.dpp, kps_x = P.hxx * P.dps;
-    const float kpp_y = P.hyy * P.dpp, kps_y = P.hyy * P.dps;
-    const float kpp_z = P.hzz * P.dpp, kps_z = P.hzz * P.dps;
-    const float dmul = P.diffusion ? 1.f : 0.f;
     const float hx2 = 0.5f * P.hx, hy2 = 0.5f * P.hy, hz2 = 0.5f * P.hz;
-    const bool row_in = y < ny && y >= P.box[2] && y < P.box[3];
+    // summation mask of this thread's 4 voxels (trimming box, inside the grid)
+    uint32_t xmask = 0;
+#pragma unroll
+    for (int i = 0; i < QX; ++i)
+        if (xb + i < nx && xb + i >= P.box[0] && xb + i < P.box[1]) xmask |= 1u << i;
+    const bool row_sum = y < ny && y >= P.box[2] && y < P.box[3];
+    const bool row_ok = y < ny;
+    // threads holding a domain face in x or y take the slow path that zeroes
+    // the weight of that face (the copy ghost gives a zero difference)
+    const bool xy_edge = (xb == 0) || (xb + QX >= nx) || (y == 0) || (y == ny - 1);
 
     Acc<float> acc[3];
-    float below[3][QX], cur[3][QX], above[3][QX];
-    float vzlo[QX] = {0.f, 0.f, 0.f, 0.f}, vzhi[QX] = {0.f, 0.f, 0.f, 0.f};
+    float prv[3][QX], cur[3][QX], nxt[3][QX];
+    float vzc[QX] = {0.f, 0.f, 0.f, 0.f}, vzp[QX] = {0.f, 0.f, 0.f, 0.f}, vzn[QX] = {0.f, 0.f, 0.f, 0.f};
 
     auto own = [&](int slot, float (&dst)[3][QX]) {
         const float* st = reinterpret_cast<const float*>(smem + slot * STAGE + OFF_STATE);
@@ -205,48 +225,50 @@ __global__ void __launch_bounds__(tma::NT, 2)
             dst[c][0] = v.x; dst[c][1] = v.y; dst[c][2] = v.z; dst[c][3] = v.w;
         }
     };
+    auto own_vz = [&](int slot, float (&dst)[QX]) {
+        if constexpr (VEL) {
+            const float4 v = *reinterpret_cast<const float4*>(smem + slot * STAGE + OFF_VZ + 4 * (w * TW + QX * lane));
+            dst[0] = v.x; dst[1] = v.y; dst[2] = v.z; dst[3] = v.w;
+        }
+    };
     bool ok = true;
-    uint32_t uses[NSTAGE] = {0u, 0u, 0u};
-    auto wait_slot = [&](int q) {  // q: plane index relative to z0-1
+    auto wait_slot = [&](int q) {
         const int slot = q % NSTAGE;
-        if (!mbar_wait(&bars[slot], uses[slot] & 1u)) ok = false;
-        uses[slot]++;
+        if (!mbar_wait(&bars[slot], (uint32_t)(q / NSTAGE) & 1u)) ok = false;
         return slot;
     };
 
-    // prologue: below (plane z0-1) and cur (plane z0)
+    // prologue: the ghost-side plane (q = 0) and the first plane (q = 1)
     if (!empty) {
-        const int sb = wait_slot(0);
-        own(sb, below);
-        const int sc = wait_slot(1);
-        own(sc, cur);
-        if constexpr (VEL) {
-            const float4 v = *reinterpret_cast<const float4*>(smem + sc * STAGE + OFF_VZ + 4 * (w * TW + QX * lane));
-            vzlo[0] = v.x; vzlo[1] = v.y; vzlo[2] = v.z; vzlo[3] = v.w;
-        }
+        const int s0 = wait_slot(0);
+        own(s0, prv);
+        own_vz(s0, vzp);
+        const int s1 = wait_slot(1);
+        own(s1, cur);
+        own_vz(s1, vzc);
         if (!ok) s_flags[0] = 1;
         __syncthreads();
         if (s_flags[0]) goto abort;
         if (tid == 0 && nplanes > NSTAGE) {
             fence_proxy_async();
-            issue(sb, z0 - 1 + NSTAGE);
-            issued[sb]++;
+            issue(s0, plane_of(NSTAGE));
+            n_issued++;
         }
     }
 
-    for (int z = z0; z < z1; ++z) {
-        const int q = z - (z0 - 1);
+    for (int q = 1; q + 1 < nplanes; ++q) {
+        const int z = plane_of(q);
         const int sc = q % NSTAGE;
-        const int sa_ = wait_slot(q + 1);
-        own(sa_, above);
-        if constexpr (VEL) {
-            const float4 v = *reinterpret_cast<const float4*>(smem + sa_ * STAGE + OFF_VZ + 4 * (w * TW + QX * lane));
-            vzhi[0] = v.x; vzhi[1] = v.y; vzhi[2] = v.z; vzhi[3] = v.w;
-        }
+        const int sn = wait_slot(q + 1);
+        own(sn, nxt);
+        own_vz(sn, vzn);
         if (!ok) s_flags[0] = 1;
+        // one instance of the plane body per marching direction, so that
+        // below / above and the upper face velocity bind to fixed registers
+        auto body = [&](const float(&bel)[3][QX], const float(&abv)[3][QX], const float(&whi)[QX]) {
+        const float(&wlo)[QX] = vzc;  // face z; whi is face z+1
         const unsigned char* base = smem + sc * STAGE;
         const float* st = reinterpret_cast<const float*>(base + OFF_STATE);
-        // neighbours in the plane
         float xm[3][QX], xp[3][QX], ym[3][QX], yp[3][QX];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -274,40 +296,35 @@ __global__ void __launch_bounds__(tma::NT, 2)
             vyl[0] = b.x; vyl[1] = b.y; vyl[2] = b.z; vyl[3] = b.w;
             vyh[0] = c.x; vyh[1] = c.y; vyh[2] = c.z; vyh[3] = c.w;
         }
-        float2 ez = make_float2(1.f, 0.f);
-        if constexpr (SCHEME == SCHEME_KSPACE) ez = s_ez[z - z0];
-        const bool zin = z >= P.box[4] && z < P.box[5];
+        const bool edge = xy_edge || z == 0 || z == nz - 1;
+        const uint32_t smask = (row_sum && z >= P.box[4] && z < P.box[5]) ? xmask : 0u;
         float o[3][QX];
+        float sx_r = 0.f, sx_i = 0.f, sz_ = 0.f;  // this plane's sums over the 4 voxels
 #pragma unroll
         for (int i = 0; i < QX; ++i) {
-            const int x = xb + i;
-            const uint32_t cd = (code4 >> (8 * i)) & 0xffu;
-            o[0][i] = 0.f; o[1][i] = 0.f; o[2][i] = 0.f;
-            if (!(cd & CODE_PORE) || x >= nx || y >= ny) continue;
-            const int f = cd & 63;
-            const float dtt1 = s_dtt1[f], dtt2 = s_dtt2[f];
-            // face weights: coefficient of (M_face - M_0)
-            float wxm = dmul * ((f & 1) ? kps_x : kpp_x), wxp = dmul * ((f & 2) ? kps_x : kpp_x);
-            float wym = dmul * ((f & 4) ? kps_y : kpp_y), wyp = dmul * ((f & 8) ? kps_y : kpp_y);
-            float wzm = dmul * ((f & 16) ? kps_z : kpp_z), wzp = dmul * ((f & 32) ? kps_z : kpp_z);
+            const uint32_t cd = (code4 >> (8 * i)) & 127u;
+            const float4 ta = s_tab[2 * cd], tb = s_tab[2 * cd + 1];
+            float wxm = ta.x, wxp = ta.y, wym = ta.z, wyp = ta.w, wzm = tb.x, wzp = tb.y;
+            const float dtt1 = tb.z, dtt2 = tb.w;
             if constexpr (VEL) {
-                const float um = vxf[i], up = vxf[i + 1], vm = vyl[i], vp = vyh[i], wm = vzlo[i], wp = vzhi[i];
-                const float u = 0.5f * (um + up), v = 0.5f * (vm + vp), ww = 0.5f * (wm + wp);
-                const float ud = fabsf(u), vd = fabsf(v), wd = fabsf(ww);
-                wxp -= hx2 * (u - ud) * upsw(up);
-                wxm += hx2 * (u + ud) * upsw(um);
-                wyp -= hy2 * (v - vd) * upsw(vp);
-                wym += hy2 * (v + vd) * upsw(vm);
-                wzp -= hz2 * (ww - wd) * upsw(wp);
-                wzm += hz2 * (ww + wd) * upsw(wm);
+                // upwind: +face -h min(u,0) s+, -face +h max(u,0) s-, u the cell average
+                const float ux = hx2 * (vxf[i] + vxf[i + 1]), uy = hy2 * (vyl[i] + vyh[i]), uz = hz2 * (wlo[i] + whi[i]);
+                wxp -= vxf[i + 1] != 0.f ? fminf(ux, 0.f) : 0.f;
+                wxm += vxf[i] != 0.f ? fmaxf(ux, 0.f) : 0.f;
+                wyp -= vyh[i] != 0.f ? fminf(uy, 0.f) : 0.f;
+                wym += vyl[i] != 0.f ? fmaxf(uy, 0.f) : 0.f;
+                wzp -= whi[i] != 0.f ? fminf(uz, 0.f) : 0.f;
+                wzm += wlo[i] != 0.f ? fmaxf(uz, 0.f) : 0.f;
             }
-            // domain faces: the copy ghost gives a zero difference
-            if (x == 0) wxm = 0.f;
-            if (x == nx - 1) wxp = 0.f;
-            if (y == 0) wym = 0.f;
-            if (y == ny - 1) wyp = 0.f;
-            if (z == 0) wzm = 0.f;
-            if (z == nz - 1) wzp = 0.f;
+            if (edge) {
+                const int x = xb + i;
+                if (x == 0) wxm = 0.f;
+                if (x >= nx - 1) wxp = 0.f;
+                if (y == 0) wym = 0.f;
+                if (y >= ny - 1) wyp = 0.f;
+                if (z == 0) wzm = 0.f;
+                if (z == nz - 1) wzp = 0.f;
+            }
             const float wsum = ((wxm + wxp) + (wym + wyp)) + (wzm + wzp);
             const float px0 = cur[0][i], py0 = cur[1][i], pz0 = cur[2][i];
             float ax, ay, az;
@@ -318,76 +335,93 @@ __global__ void __launch_bounds__(tma::NT, 2)
                 ay = py0 + dtt1 * (P.peqn[1] - divy) + dtt2 * (divy - py0);
                 az = pz0 + dtt1 * (P.peqn[2] - divz) + dtt2 * (divz - pz0);
                 if constexpr (PREC) {
-                    const float bbxb = P.b * (gdx * ((float)x + 0.5f));
+                    const float bbxb = P.b * (gdx * ((float)(xb + i) + 0.5f));
                     const float bbyb = P.b * (gdy * ((float)y + 0.5f));
                     const float bbzb = P.b * (gdz * ((float)z + 0.5f));
                     ax += bbzb * py0 - bbyb * pz0;
                     ay += bbxb * pz0 - bbzb * px0;
                     az += bbyb * px0 - bbxb * py0;
                 }
-                ax += wxm * xm[0][i] + wxp * xp[0][i] + wym * ym[0][i] + wyp * yp[0][i] + wzm * below[0][i] +
-                      wzp * above[0][i] - wsum * px0;
-                ay += wxm * xm[1][i] + wxp * xp[1][i] + wym * ym[1][i] + wyp * yp[1][i] + wzm * below[1][i] +
-                      wzp * above[1][i] - wsum * py0;
+                ax += wxm * xm[0][i] + wxp * xp[0][i] + wym * ym[0][i] + wyp * yp[0][i] + wzm * bel[0][i] +
+                      wzp * abv[0][i] - wsum * px0;
+                ay += wxm * xm[1][i] + wxp * xp[1][i] + wym * ym[1][i] + wyp * yp[1][i] + wzm * bel[1][i] +
+                      wzp * abv[1][i] - wsum * py0;
             } else {
                 ax = px0 - dtt2 * px0;
                 ay = py0 - dtt2 * py0;
                 az = pz0 + dtt1 * (P.peqn[2] - pz0);
-                // transverse: sum_f w_f (phi_f m_f) - W m_0, phi_f the face phase of this step
-                const float nbr[6] = {xm[0][i], xp[0][i], ym[0][i], yp[0][i], below[0][i], above[0][i]};
-                const float nbi[6] = {xm[1][i], xp[1][i], ym[1][i], yp[1][i], below[1][i], above[1][i]};
-                const float wf[6] = {wxm, wxp, wym, wyp, wzm, wzp};
-                float sr = -wsum * px0, si_ = -wsum * py0;
-#pragma unroll
-                for (int f6 = 0; f6 < 6; ++f6) {
-                    const float cr = wf[f6] * ph[f6][0], ci = wf[f6] * ph[f6][1];
-                    sr += cr * nbr[f6] - ci * nbi[f6];
-                    si_ += cr * nbi[f6] + ci * nbr[f6];
-                }
-                ax += sr;
-                ay += si_;
+                // per axis: w- e^{+i th} m- + w+ e^{-i th} m+
+                //   = cos th (p + q) + i sin th (p - q),  p = w- m-, q = w+ m+
+                auto axis = [&](float wm, float wp, float mr, float mi, float pr_, float pi_, float c, float s_,
+                                float& accr, float& acci) {
+                    const float pr = wm * mr, pi = wm * mi, qr = wp * pr_, qi = wp * pi_;
+                    const float ar = pr + qr, ai = pi + qi, br = pr - qr, bi = pi - qi;
+                    accr += c * ar - s_ * bi;
+                    acci += c * ai + s_ * br;
+                };
+                float tr = -wsum * px0, ti = -wsum * py0;
+                axis(wxm, wxp, xm[0][i], xm[1][i], xp[0][i], xp[1][i], ph[0][0], ph[0][1], tr, ti);
+                axis(wym, wyp, ym[0][i], ym[1][i], yp[0][i], yp[1][i], ph[1][0], ph[1][1], tr, ti);
+                axis(wzm, wzp, bel[0][i], bel[1][i], abv[0][i], abv[1][i], ph[2][0], ph[2][1], tr, ti);
+                ax += tr;
+                ay += ti;
             }
-            az += wxm * xm[2][i] + wxp * xp[2][i] + wym * ym[2][i] + wyp * yp[2][i] + wzm * below[2][i] +
-                  wzp * above[2][i] - wsum * pz0;
-            o[0][i] = ax;
-            o[1][i] = ay;
-            o[2][i] = az;
-            if (row_in && zin && x >= P.box[0] && x < P.box[1]) {
-                if constexpr (SCHEME == SCHEME_KSPACE) {
-                    const float2 ex = s_ex[QX * lane + i], ey = s_ey[w];
-                    const float xyr = ex.x * ey.x - ex.y * ey.y, xyi = ex.x * ey.y + ex.y * ey.x;
-                    const float er = xyr * ez.x - xyi * ez.y, ei = xyr * ez.y + xyi * ez.x;
-                    acc[0].add(er * ax - ei * ay);
-                    acc[1].add(er * ay + ei * ax);
-                } else {
-                    acc[0].add(ax);
-                    acc[1].add(ay);
-                }
-                acc[2].add(az);
+            az += wxm * xm[2][i] + wxp * xp[2][i] + wym * ym[2][i] + wyp * yp[2][i] + wzm * bel[2][i] +
+                  wzp * abv[2][i] - wsum * pz0;
+            const bool pore = cd & CODE_PORE;
+            o[0][i] = pore ? ax : 0.f;
+            o[1][i] = pore ? ay : 0.f;
+            o[2][i] = pore ? az : 0.f;
+            const bool take = (smask >> i) & 1u;
+            const float mr = take ? o[0][i] : 0.f, mi = take ? o[1][i] : 0.f;
+            if constexpr (SCHEME == SCHEME_KSPACE) {
+                sx_r += exr[i] * mr - exi[i] * mi;
+                sx_i += exr[i] * mi + exi[i] * mr;
+            } else {
+                sx_r += mr;
+                sx_i += mi;
             }
+            sz_ += take ? o[2][i] : 0.f;
         }
-        if (y < ny && xb < nx) {
+        if constexpr (SCHEME == SCHEME_KSPACE) {
+            // lab frame: multiply the row sum by exp(-i k_y y) exp(-i k_z z)
+            const float2 ey = s_ey[w], ez = s_ez[z - z0];
+            const float er = ey.x * ez.x - ey.y * ez.y, ei = ey.x * ez.y + ey.y * ez.x;
+            acc[0].add(er * sx_r - ei * sx_i);
+            acc[1].add(er * sx_i + ei * sx_r);
+        } else {
+            acc[0].add(sx_r);
+            acc[1].add(sx_i);
+        }
+        acc[2].add(sz_);
+        if (row_ok && xb < nx) {
             const long long off = (long long)z * P.plane + (long long)y * P.pitch + xb;
 #pragma unroll
             for (int c = 0; c < 3; ++c)
                 *reinterpret_cast<float4*>(P.out[c] + off) = make_float4(o[c][0], o[c][1], o[c][2], o[c][3]);
         }
-        __syncthreads();  // every thread is done with slot sc
+        };
+        if (d > 0) body(prv, nxt, vzn);
+        else body(nxt, prv, vzp);
+        __syncthreads();  // every thread is done with slot sc and with the previous one
         if (s_flags[0]) goto abort;
         if (tid == 0 && q + NSTAGE < nplanes) {
             fence_proxy_async();
-            issue(sc, z0 - 1 + q + NSTAGE);
-            issued[sc]++;
+            issue(sc, plane_of(q + NSTAGE));
+            n_issued++;
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
             for (int i = 0; i < QX; ++i) {
-                below[c][i] = cur[c][i];
-                cur[c][i] = above[c][i];
+                prv[c][i] = cur[c][i];
+                cur[c][i] = nxt[c][i];
             }
 #pragma unroll
-        for (int i = 0; i < QX; ++i) vzlo[i] = vzhi[i];
+        for (int i = 0; i < QX; ++i) {
+            vzp[i] = vzc[i];
+            vzc[i] = vzn[i];
+        }
     }
 
     // ---- deterministic M(t) reduction (as step_kernel) ----
@@ -455,12 +489,11 @@ abort:
     // so no TMA writes into released shared memory, and leave the counter
     if (tid == 0) {
         atomicOr(&P.ctl->status, 8);
-        for (int s = 0; s < NSTAGE; ++s) {
-            // copies still in flight on slot s complete phases uses[s] .. issued[s]-1
-            for (uint32_t k = uses[s]; k < (uint32_t)issued[s]; ++k)
-                for (uint32_t i = 0; i < WAIT_LIMIT; ++i)
-                    if (mbar_try_wait(&bars[s], k & 1u)) break;
-        }
+        // the last NSTAGE planes issued may still be in flight: wait (bounded)
+        // for the latest phase of each slot
+        for (int q = max(0, n_issued - NSTAGE); q < n_issued; ++q)
+            for (uint32_t i = 0; i < WAIT_LIMIT; ++i)
+                if (mbar_try_wait(&bars[q % NSTAGE], (uint32_t)(q / NSTAGE) & 1u)) break;
     }
     __syncthreads();
 }
