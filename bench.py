@@ -10,7 +10,7 @@ complex Mxy + Mz in FP32 (k-space exact-precession scheme), dx = 1 um,
 D = 2.3e-9 m^2/s, T1 = 2.5 s, T2 = 2.0 s, rho = 10 um/s, dt = 0.9 dx^2/(6D).
 Seeded synthetic inputs stand in for the reference's missing Poro/Vx/Vy/Vz.
 
-One bench step = STEPS_PER_ITER (100) time steps of the whole field (one
+One bench step = STEPS_PER_ITER (500) time steps of the whole field (one
 M(t) sample per time step). Every time step streams ~620 MB through HBM, so
 the working set exceeds the 129 MB L2 between timed iterations.
 
@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 METRIC = "voxel-steps/s/GB300 (%HBM roofline)"
 UNIT = "voxel-steps/s"
 SHAPE = (256, 256, 256)
-STEPS_PER_ITER = 100
+STEPS_PER_ITER = 500
 BYTES_PER_VOXEL_STEP = 37  # FP32: state read 12 + write 12 + face velocities 12 + geometry code 1
 SEED = 20261203
 WORKLOAD = "C2: 256^3 sphere pack r=10 phi_s=0.4, curl-noise flow 1 mm/s, PGSE z G=0.1 T/m d=2 ms D=20 ms, FP32 Mxy+Mz"
@@ -72,7 +72,7 @@ def physics(total_steps):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -85,7 +85,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()

@@ -277,8 +277,14 @@ __global__ void __launch_bounds__(tma::NT, 2)
             const float4 b = *reinterpret_cast<const float4*>(row + SW);
             ym[c][0] = a.x; ym[c][1] = a.y; ym[c][2] = a.z; ym[c][3] = a.w;
             yp[c][0] = b.x; yp[c][1] = b.y; yp[c][2] = b.z; yp[c][3] = b.w;
-            xm[c][0] = row[-1];
-            xp[c][3] = row[4];
+            // x halo from the neighbouring lanes; only the tile edges read shared
+            // memory (a stride-16-byte scalar load by every lane conflicts 4 ways)
+            float l = __shfl_up_sync(0xffffffffu, cur[c][QX - 1], 1);
+            float r = __shfl_down_sync(0xffffffffu, cur[c][0], 1);
+            if (lane == 0) l = row[-1];
+            if (lane == 31) r = row[QX];
+            xm[c][0] = l;
+            xp[c][QX - 1] = r;
 #pragma unroll
             for (int i = 1; i < QX; ++i) xm[c][i] = cur[c][i - 1];
 #pragma unroll
@@ -289,7 +295,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
         if constexpr (VEL) {
             const float* vxr = reinterpret_cast<const float*>(base + OFF_VX) + w * VXW + QX * lane;
             const float4 a = *reinterpret_cast<const float4*>(vxr);
-            vxf[0] = a.x; vxf[1] = a.y; vxf[2] = a.z; vxf[3] = a.w; vxf[4] = vxr[4];
+            vxf[0] = a.x; vxf[1] = a.y; vxf[2] = a.z; vxf[3] = a.w;
+            float r = __shfl_down_sync(0xffffffffu, a.x, 1);
+            if (lane == 31) r = vxr[QX];
+            vxf[QX] = r;
             const float* vyr = reinterpret_cast<const float*>(base + OFF_VY) + w * TW + QX * lane;
             const float4 b = *reinterpret_cast<const float4*>(vyr);
             const float4 c = *reinterpret_cast<const float4*>(vyr + TW);
