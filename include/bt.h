@@ -32,6 +32,7 @@ extern "C" {
 #define BT_E_STATE (-4)    /* call out of order (e.g. run before geometry) */
 #define BT_E_NOMEM (-5)    /* device allocation failed */
 #define BT_E_TIMEOUT (-6)  /* a bounded device wait gave up */
+#define BT_E_SIZE (-7)     /* grid larger than the allocation-free entry point's limit */
 
 /* precision of the fields and of the per-step arithmetic */
 #define BT_F32 0
@@ -144,6 +145,36 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit);
 /* Number of kernel launches this handle has issued (a launch inside a replayed
  * CUDA graph counts once per replay). */
 long long bt_launch_count(const bt_handle* h);
+
+/* Limits of bt_step_noalloc: its scratch is a fixed array compiled into the
+ * library (about 2.4 MB on every device that loads it). */
+#define BT_NOALLOC_MAX_VOXELS (1 << 21)   /* nx*ny*nz, e.g. 128^3 */
+#define BT_NOALLOC_MAX_BLOCKS 16384       /* CTAs of the step kernel's grid */
+
+/* One step of the REFERENCE-scheme update (the fused kernel bt_run uses for
+ * FP64 and for pulse steps) that performs no device allocation. No
+ * counterpart in the reference: it exists for callers that may not call
+ * cudaMalloc — code running under CUDA stream capture, hosts whose framework
+ * has reserved the device's memory for its own pool, plugin hosts that forbid
+ * allocations. Every buffer is the caller's device memory, dense layouts as at
+ * the top of this file, element type float (BT_F32) or double (BT_F64) per
+ * cfg->precision: mask; face velocities (NULL when cfg->velocity == 0); the
+ * field in (mx_in, my_in, mz_in) and out (must not alias the inputs); sums
+ * receives the three M(t) sums of the new field (3 doubles, device memory).
+ * The static gradient cfg->grad applies; no pulses. Asynchronous on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).
+ * The scratch (run control, schedule record, per-CTA partial sums, geometry
+ * code) is one file-scope __device__ array shared by every call on a device
+ * and keeping the last call's contents; each call re-initialises it, so calls
+ * ordered on one stream are independent, but calls that overlap on the GPU
+ * race and must not be issued. The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and should come before any
+ * stream capture. Grids above BT_NOALLOC_MAX_VOXELS voxels or
+ * BT_NOALLOC_MAX_BLOCKS blocks return BT_E_SIZE (with a message on stderr).
+ * A NaN/Inf field shows as non-finite sums (no watchdog status here). */
+int bt_step_noalloc(const bt_config* cfg, const uint8_t* mask, const void* vx, const void* vy, const void* vz,
+                    const void* mx_in, const void* my_in, const void* mz_in, void* mx_out, void* my_out,
+                    void* mz_out, double* sums, void* stream);
 
 /* ---- host-only helpers (no GPU needed) ---- */
 

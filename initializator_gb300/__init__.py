@@ -60,7 +60,7 @@ EXPORTS = [
     "bt_create", "bt_destroy", "bt_last_error", "bt_upload_geometry", "bt_set_state", "bt_get_state",
     "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
     "bt_read_mt", "bt_synchronize", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
-    "bt_version", "bt_autotune",
+    "bt_version", "bt_autotune", "bt_step_noalloc",
 ]
 
 _lib = None
@@ -98,6 +98,7 @@ def lib():
                                   ctypes.POINTER(ctypes.c_int)], i),
         "bt_version": ([], ctypes.c_char_p),
         "bt_autotune": ([vp, i, ctypes.POINTER(ctypes.c_int)], i),
+        "bt_step_noalloc": ([ctypes.POINTER(Config), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(l, name)

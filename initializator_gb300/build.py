@@ -6,6 +6,7 @@ Translation units are compiled in parallel with nvcc (one -gencode, no cmake):
 * ``bt_step_f64.cu`` — FP64 step kernels, -fmad=false so that no
   multiply-add contraction changes the reference's rounding
 * ``bt_api.cu``      — host runtime behind include/bt.h
+* ``bt_noalloc.cu``   — the allocation-free single-step entry point
 * ``bt_schedule.cpp`` — host replay of the reference's pulse schedules
 * ``host/NmrRelaxationSolve.cpp`` + ``host/nmr_io.cpp`` — the drop-in C++ class
   (linked into the same library, and into the ``nmr_exe`` program)
@@ -33,6 +34,7 @@ UNITS = [
     ("bt_step_f32.cu", ARCH + ["--ptxas-options=-v"]),
     ("bt_step_f64.cu", ARCH + ["-fmad=false"]),
     ("bt_api.cu", ARCH),
+    ("bt_noalloc.cu", ARCH),
     ("bt_schedule.cpp", []),
 ]
 HOST_UNITS = [os.path.join("host", "NmrRelaxationSolve.cpp"), os.path.join("host", "nmr_io.cpp")]
