@@ -70,6 +70,8 @@ int main(int argc, char** argv) {
     int num[3] = {1, 1, 1};
     NmrRelaxationSolve s(1, 0, num);
     s.init();
+    const double dTime_init = s.dTime;  // what StepTime derived
+    const int nStep_init = s.nStep;
     if (dt > 0) s.dTime = dt;
     const GridSize gs = s.gs;
     const size_t N = (size_t)gs.ik * gs.jk * gs.kk;
@@ -140,6 +142,8 @@ int main(int argc, char** argv) {
     std::fprintf(f, "nx %d\nny %d\nnz %d\ndTime %.17g\npEq %.17g\nnStep %d\ndirection %.17g %.17g %.17g\n",
                  gs.ik, gs.jk, gs.kk, s.dTime, s.equilibriumMagnetization, s.nStep,
                  s.direction[0], s.direction[1], s.direction[2]);
+    std::fprintf(f, "dTimeInit %.17g\nnStepInit %d\ngradientPulse %.17g\n", dTime_init, nStep_init,
+                 s.gradientPulse);
     std::fclose(f);
     return 0;
 }

@@ -11,7 +11,8 @@ outputs in ``tests/golden/<case>.npz``:
   mt                      (nsteps+1, 3) sums before every step and after the last
   state                   (3, nz, ny, nx) final field
   tau1, tau2, diff        per-voxel rates and diffusivity the reference formed
-  dt, p_eq, direction     what the reference computed in init()
+  dt, p_eq, direction     what the reference computed in init() (dt: the time step
+                          the run used; dt_init / nstep_init: StepTime's own result)
   data_*                  every Nmr_data.dat parameter
   pulses                  (n, 6) explicit AddImpulse list, empty when the case
                           runs the reference's own Sequence()
@@ -81,6 +82,8 @@ def run_case(name, data: datfiles.NmrData, mask, vel=None, grads=(2.0e-3,), nste
         "mask": mask.astype(np.uint8), "vx": vel[0], "vy": vel[1], "vz": vel[2],
         "mt": mt, "state": state, "tau1": rates[0], "tau2": rates[1], "diff": diff,
         "dt": info["dTime"][0], "p_eq": info["pEq"][0], "direction": np.array(info["direction"]),
+        "dt_init": info["dTimeInit"][0], "nstep_init": int(info["nStepInit"][0]),
+        "gradient_pulse": info["gradientPulse"][0],
         "nsteps": nsteps, "grads": np.array(grads, dtype=np.float64),
         "pulses": np.array(pulses if pulses is not None else np.zeros((0, 6)), dtype=np.float64).reshape(-1, 6),
         "state0": (np.zeros((3, nz, ny, nx)) if state0 is None else state0),

@@ -1,0 +1,82 @@
+"""The drop-in NmrRelaxationSolve (C++, initializator_gb300/csrc/host).
+
+CPU: init() reads the reference's data/*.dat files and derives the same time
+step, step count, equilibrium magnetization, field direction and gradient as
+the reference's own init() (golden fixtures record them): relative 1e-14,
+step count exact.
+GPU: nmr_exe runs the whole time loop; its CSV rows (6 significant digits, as
+the reference prints them) match the oracle run with the same time step and
+the reference's schedule to 5e-6 relative.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from dropin import describe, write_case_dir
+from helpers import CASES, common, initial_state, rel_err, velocity
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_init_matches_reference(case, tmp_path, btlib):
+    z = write_case_dir(case, str(tmp_path))
+    d = describe(str(tmp_path))
+    assert abs(d["dTime"][0] / z["dt_init"] - 1) <= 1e-14
+    assert int(d["nStep"][0]) == int(z["nstep_init"])
+    assert abs(d["pEq"][0] / z["p_eq"] - 1) <= 1e-14
+    assert np.allclose(d["direction"], z["direction"], rtol=1e-14, atol=0)
+    assert d["gradientPulse"][0] == z["gradient_pulse"]
+
+
+def _read_csv(path):
+    rows = []
+    with open(path) as f:
+        next(f)
+        for line in f:
+            rows.append([float(v) for v in line.split(";")])
+    return np.array(rows)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["fid", "pfg_flow"])
+@pytest.mark.parametrize("path", ["gpu", "cpu"])
+def test_nmr_exe_end_to_end(case, path, tmp_path, btlib, oracle_lib):
+    import initializator_gb300 as bt
+    import oracle
+    from initializator_gb300 import build
+    z = write_case_dir(case, str(tmp_path))
+    d = describe(str(tmp_path))
+    env = dict(os.environ)
+    if path == "cpu":
+        env["BT_CPU_PATH"] = "1"
+    r = subprocess.run([build.EXE, "1", "1", "1"], cwd=str(tmp_path), env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    got = _read_csv(os.path.join(str(tmp_path), f"results_{path}.csv"))
+    # the oracle with the drop-in's time step and the reference's schedule
+    dt = d["dTime"][0]
+    nstep = int(d["nStep"][0])
+    kw = common(z)
+    kw["dt"] = dt
+    pl = bt.sequence_schedule(int(z["data_n_sequence"]), nstep + 1, dt=dt, time1=float(z["data_time1"]),
+                              time2=float(z["data_time2"]), direction=tuple(z["direction"]),
+                              gradient_pulse=float(z["gradient_pulse"]), gpu_variant=(path == "gpu"))
+    p = oracle.make_params(z["mask"].shape, **kw)
+    st0 = initial_state(z)
+    s0, _ = oracle.sums(p, z["mask"], st0)
+    _, mt = oracle.run(p, z["mask"], st0, nstep + 1, vel=velocity(z), pulses=pl)
+    nd = int(z["data_nd_print"])
+    steps = np.arange(0, nstep + 1, nd)
+    ref = mt[steps] if path == "gpu" else np.vstack([s0[None], mt])[steps]
+    assert got.shape == (len(steps), 4)
+    assert np.allclose(got[:, 0], steps * dt, rtol=5e-6)
+    scale = np.abs(ref).max()
+    assert np.abs(got[:, 1:] - ref).max() <= 5e-6 * scale
+    if path == "gpu":
+        final = _read_csv_noheader(os.path.join(str(tmp_path), "results_NMR", "results_grad_1_1_1.csv"))
+        assert np.abs(final[1:] - mt[-1]).max() <= 5e-6 * scale
+
+
+def _read_csv_noheader(path):
+    with open(path) as f:
+        return np.array([float(v) for v in f.readline().split(";")])
