@@ -60,6 +60,65 @@ def build_workload(device="cpu", seed=SEED):
     return mask, vel
 
 
+QSHAPE = (256, 384, 384)   # C3a: 384 x 384 x 256
+QBATCH = 32                 # gradient strengths, linspace(0, 0.3) T/m
+QSTEPS_PER_ITER = 20
+
+
+def run_qsweep(args, lr):
+    """C3a: one 384x384x256 geometry (thresholded GRF, sigma 3, porosity 0.25),
+    flow as C2, 32 PGSE gradient strengths advanced together: one launch per
+    time step reads the shared geometry and velocity once per tile for all 32
+    fields. Algorithmic bytes per voxel-step: 24 + 13 / 32."""
+    import torch
+
+    import initializator_gb300 as bt
+    from initializator_gb300 import geometry
+    dev = torch.device("cuda", lr)
+    mask = geometry.gaussian_random_field(QSHAPE, 3.0, 0.25, seed=SEED + 7, device=dev)
+    vel = geometry.curl_velocity(mask, 4.0, 1.0e-3, seed=SEED + 8, device=dev)
+    S = QSTEPS_PER_ITER
+    total = (args.warmup + args.steps) * S + 64
+    kw, wave, rf = physics(total)
+    amps = np.linspace(0.0, 0.3, QBATCH) / 0.1   # physics() builds the 0.1 T/m waveform
+    waves = np.ascontiguousarray(wave[:, None, :] * amps[None, :, None])
+    s = bt.Solver(bt.make_config(QSHAPE, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, batch=QBATCH, **kw))
+    s.upload_geometry(mask, vel)
+    s.set_schedule(rf, grad_wave=waves)
+    m = torch.from_numpy(mask).to(dev, torch.float32)
+    st = [m.expand(QBATCH, *QSHAPE).contiguous(), torch.zeros((QBATCH,) + QSHAPE, device=dev),
+          torch.zeros((QBATCH,) + QSHAPE, device=dev)]
+    s.set_state_device(st)
+    del st, m
+    zsplit = s.autotune(8)
+    stream = torch.cuda.ExternalStream(s.stream_ptr)
+    for _ in range(args.warmup):
+        s.run_async(S)
+    s.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        s.run_async(S)
+    ev1.record(stream)
+    s.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    mt = s.read_mt(S)
+    finite = bool(np.all(np.isfinite(mt)))
+    s.close()
+    nvox = int(np.prod(QSHAPE))
+    vsteps = nvox * QBATCH * S * args.steps
+    per_launch = ms / 1e3 / (S * args.steps)
+    bytes_launch = (24 * QBATCH + 13) * nvox
+    peak, peak_kind = hbm_peak()
+    return {"workload": "C3a: 384x384x256 GRF sigma=3 porosity 0.25, flow 1 mm/s, 32 PGSE G in 0..0.3 T/m, FP32",
+            "value": vsteps / (ms / 1e3), "unit": UNIT, "ms_per_time_step": per_launch * 1e3, "batch": QBATCH,
+            "tma_zsplit": zsplit, "finite": finite,
+            "roofline": {"bound": "hbm", "achieved": bytes_launch / per_launch / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": bytes_launch / per_launch / 1e9 / peak, "peak_kind": peak_kind,
+                         "bytes_per_voxel_step": 24 + 13 / QBATCH}}
+
+
 def physics(total_steps):
     import initializator_gb300 as bt
     from initializator_gb300 import geometry
@@ -292,6 +351,7 @@ def run_ours(args):
         e2e_s = float(t.item())
     e2e = nvox * S * args.steps * w / e2e_s
     s.close()
+    qsweep = None if args.no_qsweep else run_qsweep(args, lr)
 
     out = None
     if r == 0:
@@ -312,6 +372,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": 3 * 8 * S},
             "gpu_launches": launches,
             "clocks": clk,
+            "qsweep": qsweep,
         }
         print(json.dumps(out))
     if w > 1:
@@ -327,6 +388,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-qsweep", action="store_true", help="skip the batched 32-gradient q-sweep (C3a) leg")
     ap.add_argument("--zsplit", type=int, default=0, help="fixed z-chunking of the fast path (skips the autotuner)")
     ap.add_argument("--profile", action="store_true",
                     help="device-resident phase only (for ncu captures); prints no bench line")

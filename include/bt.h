@@ -60,7 +60,7 @@ typedef struct bt_config {
     int velocity;          /* NVELOC: 1 = advection on */
     int diffusion;         /* NDIFFUS: 1 = diffusion on */
     int buffer[3];         /* bufferX/Y/Z: cells trimmed from each side of the M(t) sums */
-    int reserved;
+    int batch;             /* fields advanced together over one geometry (a q-sweep); 0 or 1 = one */
     double dx, dy, dz;     /* voxel edges, m */
     double dt;             /* time step, s */
     double main_field[3];  /* mainField vector (FillInMainField, cpp:1944-1962); its unit vector is n */
@@ -99,6 +99,13 @@ const char* bt_last_error(const bt_handle* h);
  * cpp:819-878, 1435-1536, 1756-1893). vx/vy/vz may be NULL when velocity == 0. */
 int bt_upload_geometry(bt_handle* h, const uint8_t* mask,
                        const double* vx, const double* vy, const double* vz);
+
+/* Batches (cfg->batch = B > 1): B fields share the geometry and flow and
+ * advance together, each with its own gradient waveform (a q-sweep; the
+ * reference runs one process per gradient, main.cpp:16-28). Field arrays then
+ * hold B consecutive fields per component ([B][nz][ny][nx]), grad_wave is
+ * [nwave][B][3], M(t) outputs are [nsteps][B][3] and bt_measure writes 3*B
+ * sums; pulses apply to every member. */
 
 /* Whole field in / out in the lab frame (replaces FillInMagnetization,
  * cpp:2472-2517, and the D2H copies of solve_gpu, cu:1193-1201). */

@@ -36,7 +36,7 @@ class Config(ctypes.Structure):
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
         ("precision", ctypes.c_int), ("scheme", ctypes.c_int),
         ("vector_mult", ctypes.c_int), ("velocity", ctypes.c_int), ("diffusion", ctypes.c_int),
-        ("buffer", ctypes.c_int * 3), ("reserved", ctypes.c_int),
+        ("buffer", ctypes.c_int * 3), ("batch", ctypes.c_int),
         ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
         ("main_field", ctypes.c_double * 3), ("gamma", ctypes.c_double), ("grad", ctypes.c_double * 3),
         ("d_pore", ctypes.c_double), ("t1", ctypes.c_double), ("t2", ctypes.c_double),
@@ -115,9 +115,10 @@ def _dp(a):
 def make_config(shape, *, dx, dy=None, dz=None, dt, precision=BT_F32, scheme=BT_SCHEME_REFERENCE,
                 main_field=(1.0, 0.0, 0.0), gamma=GAMMA_REFERENCE, grad=(0.0, 0.0, 0.0), d_pore=2.3e-9,
                 t1=2.5, t2=2.0, rho1=0.0, rho2=0.0, p_eq=1.0, vector_mult=0, velocity=0, diffusion=1,
-                buffer=(0, 0, 0)) -> Config:
+                buffer=(0, 0, 0), batch=1) -> Config:
     nz, ny, nx = shape
     c = Config()
+    c.batch = batch
     c.nx, c.ny, c.nz = nx, ny, nz
     c.precision, c.scheme = precision, scheme
     c.vector_mult, c.velocity, c.diffusion = vector_mult, velocity, diffusion
@@ -162,6 +163,7 @@ class Solver:
             raise BtError(rc, "bt_create failed")
         self._h = h
         self.shape = (cfg.nz, cfg.ny, cfg.nx)
+        self.batch = max(1, cfg.batch)
 
     def _check(self, rc, what):
         if rc:
@@ -197,7 +199,9 @@ class Solver:
                         "upload_geometry")
 
     def set_state(self, state):
-        st = [np.ascontiguousarray(state[c], dtype=np.float64) for c in range(3)]
+        """state: (3, nz, ny, nx), or (B, 3, nz, ny, nx) for a batch of B fields."""
+        state = np.asarray(state, dtype=np.float64).reshape((self.batch, 3) + self.shape)
+        st = [np.ascontiguousarray(state[:, c]) for c in range(3)]
         self._check(self._l.bt_set_state(self._h, _dp(st[0]), _dp(st[1]), _dp(st[2])), "set_state")
 
     def set_state_device(self, tensors):
@@ -206,9 +210,10 @@ class Solver:
                     "set_state_device")
 
     def get_state(self):
-        out = np.zeros((3,) + self.shape)
-        self._check(self._l.bt_get_state(self._h, _dp(out[0]), _dp(out[1]), _dp(out[2])), "get_state")
-        return out
+        comps = [np.zeros((self.batch,) + self.shape) for _ in range(3)]
+        self._check(self._l.bt_get_state(self._h, _dp(comps[0]), _dp(comps[1]), _dp(comps[2])), "get_state")
+        out = np.stack(comps, axis=1)
+        return out[0] if self.batch == 1 else out
 
     def set_schedule(self, pulses=(), grad_wave=None):
         arr = (Pulse * max(1, len(pulses)))()
@@ -218,7 +223,7 @@ class Solver:
         gw = None
         nwave = 0
         if grad_wave is not None:
-            gw = np.ascontiguousarray(grad_wave, dtype=np.float64).reshape(-1, 3)
+            gw = np.ascontiguousarray(grad_wave, dtype=np.float64).reshape(-1, self.batch, 3)
             nwave = gw.shape[0]
         self._check(self._l.bt_set_schedule(self._h, arr, len(pulses), _dp(gw), nwave), "set_schedule")
 
@@ -230,17 +235,18 @@ class Solver:
         self._check(self._l.bt_set_step(self._h, int(step)), "set_step")
 
     def run(self, nsteps):
-        mt = np.zeros((max(1, nsteps), 3))
+        """Advance nsteps; M(t) after each step: (nsteps, 3), or (nsteps, B, 3)."""
+        mt = np.zeros((max(1, nsteps), self.batch, 3))
         self._check(self._l.bt_run(self._h, int(nsteps), _dp(mt)), "run")
-        return mt[:nsteps]
+        return mt[:nsteps, 0] if self.batch == 1 else mt[:nsteps]
 
     def run_async(self, nsteps):
         self._check(self._l.bt_run_async(self._h, int(nsteps)), "run_async")
 
     def read_mt(self, nsteps):
-        mt = np.zeros((max(1, nsteps), 3))
+        mt = np.zeros((max(1, nsteps), self.batch, 3))
         self._check(self._l.bt_read_mt(self._h, _dp(mt), int(nsteps)), "read_mt")
-        return mt[:nsteps]
+        return mt[:nsteps, 0] if self.batch == 1 else mt[:nsteps]
 
     def synchronize(self):
         self._check(self._l.bt_synchronize(self._h), "synchronize")
@@ -250,9 +256,9 @@ class Solver:
         return self._l.bt_stream(self._h)
 
     def measure(self):
-        out = np.zeros(3)
+        out = np.zeros((self.batch, 3))
         self._check(self._l.bt_measure(self._h, _dp(out)), "measure")
-        return out
+        return out[0] if self.batch == 1 else out
 
     def autotune(self, trial_steps=64):
         """Time the candidate z-splits of the FP32 fast path; returns the chosen one."""

@@ -39,7 +39,10 @@ struct bt_handle {
     size_t nvox = 0;              // nx*ny*nz
     int pitch = 0, vxpitch = 0, cpitch = 0;
     size_t comp = 0;              // elements per component (pitch*ny*nz)
-    void* state_base[2] = {};     // one allocation of 3 components per ping-pong side
+    int nb = 1;                   // fields advanced together (batch members)
+    int gzsplit = 1;              // z-chunks per field, generic kernel
+    int tzsplit = 1;              // z-chunks per field, TMA kernel
+    void* state_base[2] = {};     // one allocation per ping-pong side: [batch][component][z][y][pitch]
     void* state[2][3] = {};
     int cur = 0;
     uint8_t* code = nullptr;
@@ -48,7 +51,7 @@ struct bt_handle {
     bt::StepInfo* steps_d = nullptr;
     long long nsched = 0;
     std::vector<bt::StepInfo> steps_h;
-    std::vector<double> kpos;     // wave vector at the start of each step (KSPACE), 3 per step
+    std::vector<double> kpos;     // wave vector at the start of each step (KSPACE): [step][batch][3]
     bt::DevPulse* pulses_d = nullptr;
     bt::Ctl* ctl_d = nullptr;
     bt::Ctl* ctl_h = nullptr;     // pinned
@@ -114,7 +117,7 @@ __global__ void code_kernel(const uint8_t* mask, uint8_t* code, int nx, int ny, 
 }
 
 template <typename T>
-void fill_params(bt_handle* h, bt::StepParams<T>* p, dim3 grid) {
+void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
     const bt_config& c = h->cfg;
     const double dTime = c.dt;
     const double Bx = c.main_field[0], By = c.main_field[1], Bz = c.main_field[2];
@@ -132,8 +135,10 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, dim3 grid) {
         P.nx = c.nx; P.ny = c.ny; P.nz = c.nz;
         P.pitch = h->pitch; P.vxpitch = h->vxpitch; P.cpitch = h->cpitch;
         P.plane = (long long)h->pitch * c.ny;
-        P.zsplit = (int)grid.z;
+        P.zsplit = zsplit;
         P.zchunk = (c.nz + P.zsplit - 1) / P.zsplit;
+        P.nbatch = h->nb;
+        P.bstride = 3LL * (long long)h->comp;
         for (int k = 0; k < 3; ++k) {
             P.in[k] = static_cast<const T*>(h->state[s][k]);
             P.out[k] = static_cast<T*>(h->state[1 - s][k]);
@@ -183,10 +188,10 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, dim3 grid) {
 
 void refresh_params(bt_handle* h) {
     if (h->cfg.precision == BT_F64) {
-        fill_params<double>(h, h->pd, h->grid);
+        fill_params<double>(h, h->pd, h->gzsplit);
     } else {
-        fill_params<float>(h, h->pf, h->grid);
-        fill_params<float>(h, h->pt, dim3(1, 1, h->tgrid.x));
+        fill_params<float>(h, h->pf, h->gzsplit);
+        fill_params<float>(h, h->pt, h->tzsplit);
     }
     drop_graphs(h);
 }
@@ -208,7 +213,7 @@ bool encode(CUtensorMap* m, CUtensorMapDataType t, int rank, void* base, const c
             const cuuint64_t* strides, const cuuint32_t* box) {
     auto fn = encoder();
     if (!fn) return false;
-    cuuint32_t es[4] = {1, 1, 1, 1};
+    cuuint32_t es[5] = {1, 1, 1, 1, 1};
     return fn(m, t, rank, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -222,10 +227,10 @@ bool build_maps(bt_handle* h) {
         bt::TmaMaps& M = h->maps[s];
         std::memset(&M, 0, sizeof(M));
         {
-            cuuint64_t dims[4] = {nx, ny, nz, 3};
-            cuuint64_t str[3] = {P4, P4 * ny, (cuuint64_t)h->comp * 4};
-            cuuint32_t box[4] = {bt::TMA_TX + 8, bt::TMA_TY + 2, 1, 3};
-            if (!encode(&M.state, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->state_base[s], dims, str, box)) return false;
+            cuuint64_t dims[5] = {nx, ny, nz, 3, (cuuint64_t)h->nb};
+            cuuint64_t str[4] = {P4, P4 * ny, (cuuint64_t)h->comp * 4, (cuuint64_t)h->comp * 12};
+            cuuint32_t box[5] = {bt::TMA_TX + 8, bt::TMA_TY + 2, 1, 3, 1};
+            if (!encode(&M.state, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, h->state_base[s], dims, str, box)) return false;
         }
         {
             cuuint64_t dims[3] = {nx, ny, nz};
@@ -260,8 +265,9 @@ int set_tma_split(bt_handle* h, int zsplit) {
     const bt_config& c = h->cfg;
     zsplit = normalise_split(c.nz, zsplit);
     const int gx = (c.nx + bt::TMA_TX - 1) / bt::TMA_TX, gy = (c.ny + bt::TMA_TY - 1) / bt::TMA_TY;
-    h->tgrid = dim3(zsplit, gx, gy);
-    const size_t need = 3 * (size_t)zsplit * gx * gy;
+    h->tzsplit = zsplit;
+    h->tgrid = dim3(zsplit * h->nb, gx, gy);
+    const size_t need = 3 * (size_t)zsplit * gx * gy * h->nb;
     if (need > h->partials_cap) {
         if (h->partials_d) cudaFree(h->partials_d);
         h->partials_d = nullptr;
@@ -276,7 +282,8 @@ int set_tma_split(bt_handle* h, int zsplit) {
 // default split: about 4 waves of 2 CTAs per SM, chunks of at least 8 planes
 int default_tma_split(const bt_handle* h) {
     const bt_config& c = h->cfg;
-    const long long tiles = (long long)((c.nx + bt::TMA_TX - 1) / bt::TMA_TX) * ((c.ny + bt::TMA_TY - 1) / bt::TMA_TY);
+    const long long tiles =
+        (long long)((c.nx + bt::TMA_TX - 1) / bt::TMA_TX) * ((c.ny + bt::TMA_TY - 1) / bt::TMA_TY) * h->nb;
     const long long slots = 2LL * h->num_sms;
     long long zs = (4 * slots + tiles - 1) / tiles;
     zs = std::min<long long>(zs, std::max(1, c.nz / 8));
@@ -285,7 +292,7 @@ int default_tma_split(const bt_handle* h) {
 }
 
 bool step_has_pulse(const bt_handle* h, long long s) {
-    return s < h->nsched && h->steps_h[s].pulse_count > 0;
+    return s < h->nsched && h->steps_h[s * h->nb].pulse_count > 0;
 }
 
 cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
@@ -327,34 +334,39 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
         d.naxis[0] = nx / length; d.naxis[1] = ny / length; d.naxis[2] = nz / length;
         d.eff = std::pow(nx * nx + ny * ny + nz * nz, 0.5);
     }
-    std::vector<bt::StepInfo> st(nsched + 1);
-    h->kpos.assign(3 * (nsched + 1), 0.0);
-    double k[3] = {0.0, 0.0, 0.0};
+    // one record per step and batch member ([step][member]); grad_wave is
+    // [nwave][member][3]; the members share the pulses
+    const int nb = h->nb;
+    std::vector<bt::StepInfo> st((nsched + 1) * nb);
+    h->kpos.assign(3 * (nsched + 1) * nb, 0.0);
     const double d3[3] = {c.dx, c.dy, c.dz};
-    int qi = 0;
-    for (long long s = 0; s <= nsched; ++s) {
-        bt::StepInfo& si = st[s];
-        std::memset(&si, 0, sizeof(si));
-        const bool in_wave = grad_wave && s < nwave;
-        for (int a = 0; a < 3; ++a) si.grad[a] = in_wave ? grad_wave[3 * s + a] : c.grad[a];
-        for (int a = 0; a < 3; ++a) h->kpos[3 * s + a] = k[a];
-        for (int a = 0; a < 3; ++a) {
-            // neighbour at -d: exp(+i k d); at +d: exp(-i k d)
-            const double ang = k[a] * d3[a];
-            si.phase[2 * a][0] = std::cos(ang);
-            si.phase[2 * a][1] = std::sin(ang);
-            si.phase[2 * a + 1][0] = std::cos(ang);
-            si.phase[2 * a + 1][1] = -std::sin(ang);
+    for (int b = 0; b < nb; ++b) {
+        double k[3] = {0.0, 0.0, 0.0};
+        int qi = 0;
+        for (long long s = 0; s <= nsched; ++s) {
+            bt::StepInfo& si = st[s * nb + b];
+            std::memset(&si, 0, sizeof(si));
+            const bool in_wave = grad_wave && s < nwave;
+            for (int a = 0; a < 3; ++a) si.grad[a] = in_wave ? grad_wave[3 * (s * nb + b) + a] : c.grad[a];
+            if (s == nsched)  // the default entry used beyond the table: cfg gradient, no pulses
+                for (int a = 0; a < 3; ++a) si.grad[a] = c.grad[a];
+            for (int a = 0; a < 3; ++a) h->kpos[3 * (s * nb + b) + a] = k[a];
+            for (int a = 0; a < 3; ++a) {
+                // neighbour at -d: exp(+i k d); at +d: exp(-i k d)
+                const double ang = k[a] * d3[a];
+                si.phase[2 * a][0] = std::cos(ang);
+                si.phase[2 * a][1] = std::sin(ang);
+                si.phase[2 * a + 1][0] = std::cos(ang);
+                si.phase[2 * a + 1][1] = -std::sin(ang);
+            }
+            if (c.scheme == BT_SCHEME_KSPACE && s < nsched)
+                for (int a = 0; a < 3; ++a) k[a] = k[a] + c.gamma * si.grad[a] * c.dt;
+            for (int a = 0; a < 3; ++a) si.knext[a] = k[a];
+            si.pulse_first = qi;
+            while (qi < npulses && pulses[order[qi]].step == s) qi++;
+            si.pulse_count = s < nsched ? qi - si.pulse_first : 0;
         }
-        if (c.scheme == BT_SCHEME_KSPACE && s < nsched)
-            for (int a = 0; a < 3; ++a) k[a] = k[a] + c.gamma * si.grad[a] * c.dt;
-        for (int a = 0; a < 3; ++a) si.knext[a] = k[a];
-        si.pulse_first = qi;
-        while (qi < npulses && pulses[order[qi]].step == s) qi++;
-        si.pulse_count = s < nsched ? qi - si.pulse_first : 0;
     }
-    // the default entry (index nsched) used beyond the table: no pulses, cfg gradient
-    for (int a = 0; a < 3; ++a) st[nsched].grad[a] = c.grad[a];
     if (h->steps_d) cudaFree(h->steps_d);
     if (h->pulses_d) cudaFree(h->pulses_d);
     h->steps_d = nullptr;
@@ -369,13 +381,13 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
     return BT_OK;
 }
 
-void kvec_at(const bt_handle* h, long long s, double k[3]) {
+void kvec_at(const bt_handle* h, long long s, int b, double k[3]) {
     if (h->cfg.scheme != BT_SCHEME_KSPACE || h->kpos.empty()) {
         k[0] = k[1] = k[2] = 0.0;
         return;
     }
     const long long i = std::min<long long>(s, h->nsched);
-    for (int a = 0; a < 3; ++a) k[a] = h->kpos[3 * i + a];
+    for (int a = 0; a < 3; ++a) k[a] = h->kpos[3 * (i * h->nb + b) + a];
 }
 
 int ensure_mt(bt_handle* h, long long n) {
@@ -384,7 +396,7 @@ int ensure_mt(bt_handle* h, long long n) {
     if (h->mt_d) cudaFree(h->mt_d);
     h->mt_d = nullptr;
     h->mt_cap = 0;
-    CK(h, cudaMalloc(&h->mt_d, sizeof(double) * 3 * cap));
+    CK(h, cudaMalloc(&h->mt_d, sizeof(double) * 3 * cap * h->nb));
     h->mt_cap = cap;
     refresh_params(h);
     return BT_OK;
@@ -402,24 +414,37 @@ int check_ctl(bt_handle* h) {
     return BT_OK;
 }
 
+// (x + i y) of every member's field *= exp(sign * i * k_member . r) at the current step
 int frame_change(bt_handle* h, void* const* f, int sign) {
-    double k[3];
-    kvec_at(h, h->step, k);
-    if (k[0] == 0.0 && k[1] == 0.0 && k[2] == 0.0) return BT_OK;
     const bt_config& c = h->cfg;
-    cudaError_t e;
-    if (h->esz == 8) {
-        double* fp[3] = {(double*)f[0], (double*)f[1], (double*)f[2]};
-        e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, h->pitch, h->cpitch, k[0], k[1], k[2], c.dx, c.dy,
-                                     c.dz, sign, h->stream);
-    } else {
-        float* fp[3] = {(float*)f[0], (float*)f[1], (float*)f[2]};
-        e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, h->pitch, h->cpitch, k[0], k[1], k[2], c.dx, c.dy,
-                                    c.dz, sign, h->stream);
+    for (int b = 0; b < h->nb; ++b) {
+        double k[3];
+        kvec_at(h, h->step, b, k);
+        if (k[0] == 0.0 && k[1] == 0.0 && k[2] == 0.0) continue;
+        const size_t off = (size_t)b * 3 * h->comp * h->esz;
+        cudaError_t e;
+        if (h->esz == 8) {
+            double* fp[3] = {(double*)((char*)f[0] + off), (double*)((char*)f[1] + off), (double*)((char*)f[2] + off)};
+            e = bt::launch_frame<double>(fp, h->code, c.nx, c.ny, c.nz, h->pitch, h->cpitch, k[0], k[1], k[2], c.dx,
+                                         c.dy, c.dz, sign, h->stream);
+        } else {
+            float* fp[3] = {(float*)((char*)f[0] + off), (float*)((char*)f[1] + off), (float*)((char*)f[2] + off)};
+            e = bt::launch_frame<float>(fp, h->code, c.nx, c.ny, c.nz, h->pitch, h->cpitch, k[0], k[1], k[2], c.dx,
+                                        c.dy, c.dz, sign, h->stream);
+        }
+        CK(h, e);
+        h->launches++;
     }
-    CK(h, e);
-    h->launches++;
     return BT_OK;
+}
+
+bool any_phase(const bt_handle* h) {
+    for (int b = 0; b < h->nb; ++b) {
+        double k[3];
+        kvec_at(h, h->step, b, k);
+        if (k[0] != 0.0 || k[1] != 0.0 || k[2] != 0.0) return true;
+    }
+    return false;
 }
 
 // dense [nz][ny][nx] host component <-> pitched device component
@@ -477,6 +502,7 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     h->vxpitch = round_up(cfg->nx + 1, 4);
     h->cpitch = round_up(cfg->nx, 16);
     h->comp = (size_t)h->pitch * cfg->ny * cfg->nz;
+    h->nb = cfg->batch > 1 ? cfg->batch : 1;
     int rc = BT_OK;
     auto bail = [&](int code) {
         bt_destroy(h);
@@ -488,13 +514,14 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     // generic kernel grid: 32 x 8 column tiles; z split so that the grid fills the SMs several times
     const int gx = (cfg->nx + bt::TX - 1) / bt::TX, gy = (cfg->ny + bt::TY - 1) / bt::TY;
     int zsplit = 1;
-    const long long tiles = (long long)gx * gy;
+    const long long tiles = (long long)gx * gy * h->nb;
     const long long want = 8LL * h->num_sms;
     if (tiles < want) zsplit = (int)std::min<long long>((want + tiles - 1) / tiles, std::max(1, cfg->nz / 8));
     if (const char* e = std::getenv("BT_ZSPLIT")) zsplit = std::max(1, std::atoi(e));
     zsplit = normalise_split(cfg->nz, zsplit);
-    h->grid = dim3(gx, gy, zsplit);
-    const size_t sbytes = 3 * h->esz * h->comp;
+    h->gzsplit = zsplit;
+    h->grid = dim3(gx, gy, zsplit * h->nb);  // blockIdx.z = z-chunk + zsplit * batch member
+    const size_t sbytes = 3 * h->esz * h->comp * h->nb;
     for (int s = 0; s < 2; ++s) {
         if (cudaMalloc(&h->state_base[s], sbytes) != cudaSuccess) return bail(BT_E_NOMEM);
         cudaMemset(h->state_base[s], 0, sbytes);
@@ -512,6 +539,7 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
         }
     }
     if (cfg->precision == BT_F32 && cudaMallocHost(&h->staging, 4 * h->nvox) != cudaSuccess) return bail(BT_E_NOMEM);
+    if (cfg->batch < 0 || (long long)h->nb * (long long)h->comp * 3 > (1LL << 40)) return bail(BT_E_ARG);
     const size_t nblocks = (size_t)h->grid.x * h->grid.y * h->grid.z;
     h->partials_cap = std::max<size_t>(3 * nblocks, 4 * SUMS_BLOCKS);
     if (cudaMalloc(&h->partials_d, sizeof(double) * h->partials_cap) != cudaSuccess) return bail(BT_E_NOMEM);
@@ -597,10 +625,12 @@ int bt_set_state(bt_handle* h, const double* mx, const double* my, const double*
     if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
     const double* src[3] = {mx, my, mz};
-    for (int a = 0; a < 3; ++a) {
-        int rc = put_component(h, h->state[h->cur][a], src[a]);
-        if (rc) return rc;
-    }
+    for (int b = 0; b < h->nb; ++b)
+        for (int a = 0; a < 3; ++a) {
+            void* dst = (char*)h->state[h->cur][a] + (size_t)b * 3 * h->comp * h->esz;
+            int rc = put_component(h, dst, src[a] + (size_t)b * h->nvox);
+            if (rc) return rc;
+        }
     int rc = frame_change(h, h->state[h->cur], +1);
     if (rc) return rc;
     CK(h, cudaStreamSynchronize(h->stream));
@@ -612,31 +642,34 @@ int bt_set_state_device(bt_handle* h, const void* mx, const void* my, const void
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
     const bt_config& c = h->cfg;
     const void* src[3] = {mx, my, mz};
-    for (int a = 0; a < 3; ++a)
-        CK(h, cudaMemcpy2DAsync(h->state[h->cur][a], h->pitch * h->esz, src[a], c.nx * h->esz, c.nx * h->esz,
-                                (size_t)c.ny * c.nz, cudaMemcpyDeviceToDevice, h->stream));
+    for (int b = 0; b < h->nb; ++b)
+        for (int a = 0; a < 3; ++a)
+            CK(h, cudaMemcpy2DAsync((char*)h->state[h->cur][a] + (size_t)b * 3 * h->comp * h->esz, h->pitch * h->esz,
+                                    (const char*)src[a] + (size_t)b * h->nvox * h->esz, c.nx * h->esz, c.nx * h->esz,
+                                    (size_t)c.ny * c.nz, cudaMemcpyDeviceToDevice, h->stream));
     return frame_change(h, h->state[h->cur], +1);
 }
 
 int bt_get_state(bt_handle* h, double* mx, double* my, double* mz) {
     if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
-    double k[3];
-    kvec_at(h, h->step, k);
-    const bool phase = (k[0] != 0.0 || k[1] != 0.0 || k[2] != 0.0);
+    const bool phase = any_phase(h);
     // the idle ping-pong buffer holds the lab-frame copy; the next step overwrites it
     void** src = h->state[h->cur];
     void** tmp = h->state[1 - h->cur];
     if (phase) {
-        for (int a = 0; a < 2; ++a)
-            CK(h, cudaMemcpyAsync(tmp[a], src[a], h->esz * h->comp, cudaMemcpyDeviceToDevice, h->stream));
+        CK(h, cudaMemcpyAsync(h->state_base[1 - h->cur], h->state_base[h->cur], 3 * h->nb * h->esz * h->comp,
+                              cudaMemcpyDeviceToDevice, h->stream));
         int rc = frame_change(h, tmp, -1);
         if (rc) return rc;
     }
     double* dst[3] = {mx, my, mz};
-    for (int a = 0; a < 3; ++a) {
-        int rc = get_component(h, dst[a], (phase && a < 2) ? tmp[a] : src[a]);
-        if (rc) return rc;
-    }
+    void** from = phase ? tmp : src;
+    for (int b = 0; b < h->nb; ++b)
+        for (int a = 0; a < 3; ++a) {
+            int rc = get_component(h, dst[a] + (size_t)b * h->nvox,
+                                   (const char*)from[a] + (size_t)b * 3 * h->comp * h->esz);
+            if (rc) return rc;
+        }
     return BT_OK;
 }
 
@@ -718,7 +751,7 @@ int bt_read_mt(bt_handle* h, double* mt_out, long long nsteps) {
     int rc = check_ctl(h);
     if (rc) return rc;
     if (mt_out && nsteps > 0)
-        CK(h, cudaMemcpy(mt_out, h->mt_d, sizeof(double) * 3 * nsteps, cudaMemcpyDeviceToHost));
+        CK(h, cudaMemcpy(mt_out, h->mt_d, sizeof(double) * 3 * nsteps * h->nb, cudaMemcpyDeviceToHost));
     return BT_OK;
 }
 
@@ -739,21 +772,31 @@ void* bt_stream(bt_handle* h) { return h ? (void*)h->stream : nullptr; }
 int bt_measure(bt_handle* h, double* sums3) {
     if (!h || !sums3) return fail(h, BT_E_ARG, "null output");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
-    double kv[4];
-    kvec_at(h, h->step, kv);
-    kv[3] = SUMS_BLOCKS;
-    cudaError_t e;
-    if (h->esz == 8) e = bt::launch_sums<double>(h->pd[h->cur], kv, h->stream);
-    else e = bt::launch_sums<float>(h->pf[h->cur], kv, h->stream);
-    CK(h, e);
-    h->launches++;
     std::vector<double> part(4 * SUMS_BLOCKS);
-    CK(h, cudaMemcpyAsync(part.data(), h->partials_d, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
-    double t[3] = {0.0, 0.0, 0.0};
-    for (int b = 0; b < SUMS_BLOCKS; ++b)
-        for (int a = 0; a < 3; ++a) t[a] += part[4 * b + a];
-    for (int a = 0; a < 3; ++a) sums3[a] = t[a];
+    for (int b = 0; b < h->nb; ++b) {
+        double kv[4];
+        kvec_at(h, h->step, b, kv);
+        kv[3] = SUMS_BLOCKS;
+        cudaError_t e;
+        if (h->esz == 8) {
+            bt::StepParams<double> P = h->pd[h->cur];
+            for (int a = 0; a < 3; ++a) P.in[a] += (size_t)b * 3 * h->comp;
+            e = bt::launch_sums<double>(P, kv, h->stream);
+        } else {
+            bt::StepParams<float> P = h->pf[h->cur];
+            for (int a = 0; a < 3; ++a) P.in[a] += (size_t)b * 3 * h->comp;
+            e = bt::launch_sums<float>(P, kv, h->stream);
+        }
+        CK(h, e);
+        h->launches++;
+        CK(h, cudaMemcpyAsync(part.data(), h->partials_d, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+                              h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        double t[3] = {0.0, 0.0, 0.0};
+        for (int q = 0; q < SUMS_BLOCKS; ++q)
+            for (int a = 0; a < 3; ++a) t[a] += part[4 * q + a];
+        for (int a = 0; a < 3; ++a) sums3[3 * b + a] = t[a];
+    }
     return BT_OK;
 }
 
@@ -763,12 +806,12 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
     if (!h || trial_steps <= 0) return fail(h, BT_E_ARG, "bad autotune arguments");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
     if (h->cfg.precision != BT_F32 || !h->use_tma) {
-        if (best_zsplit) *best_zsplit = (int)h->grid.z;
+        if (best_zsplit) *best_zsplit = h->gzsplit;
         return BT_OK;
     }
     // candidate z-splits: waves of 2 CTAs per SM from 1 to 8, chunks of >= 4 planes
     const bt_config& c = h->cfg;
-    const long long tiles = (long long)h->tgrid.y * h->tgrid.z;
+    const long long tiles = (long long)h->tgrid.y * h->tgrid.z * h->nb;
     std::vector<int> cand;
     for (int waves = 1; waves <= 8; ++waves) {
         const long long zs = (waves * 2LL * h->num_sms + tiles - 1) / tiles;
@@ -781,14 +824,14 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
     const long long step0 = h->step;
     const int cur0 = h->cur;
     void* keep = nullptr;
-    const size_t sbytes = 3 * h->esz * h->comp;
+    const size_t sbytes = 3 * h->esz * h->comp * h->nb;
     CK(h, cudaMalloc(&keep, sbytes));
     CK(h, cudaMemcpyAsync(keep, h->state_base[h->cur], sbytes, cudaMemcpyDeviceToDevice, h->stream));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    int best_zs = (int)h->tgrid.x;
+    int best_zs = h->tzsplit;
     int rc = BT_OK;
     for (int& zs : cand) zs = normalise_split(c.nz, zs);
     std::sort(cand.begin(), cand.end());

@@ -54,7 +54,9 @@ template <typename T>
 struct StepParams {
     int nx, ny, nz, zchunk;
     int pitch, vxpitch, cpitch;
-    int zsplit;
+    int zsplit;                 // z-chunks per field
+    int nbatch;                 // fields advanced together (q-sweep); 0 or 1 = one
+    long long bstride;          // elements from one batch member's field to the next
     long long plane;            // pitch * ny (state and vz plane stride)
     const T* in[3];
     T* out[3];
@@ -74,13 +76,13 @@ struct StepParams {
     int diffusion;
     int box[6];                 // M(t) trimming box [x0,x1) [y0,y1) [z0,z1)
     double dxd, dyd, dzd, gamma;  // FP64 copies for pulse angles and k phases
-    const StepInfo* steps;
-    long long nsched;           // entries in steps (steps[nsched] is the default)
+    const StepInfo* steps;      // [(nsched + 1) * nbatch], step-major
+    long long nsched;           // steps in the table (entry nsched is the default)
     const DevPulse* pulses;
     Ctl* ctl;
-    double* partials;           // [gridDim x*y*z][3]
-    double* mt;                 // [mt_cap][3]
-    long long mt_cap;
+    double* partials;           // [nbatch][CTAs per member][3]
+    double* mt;                 // [mt_cap][nbatch][3]
+    long long mt_cap;           // steps
 };
 
 // TMA descriptors of the FP32 fast path (one per ping-pong input side)

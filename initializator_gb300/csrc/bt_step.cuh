@@ -120,6 +120,81 @@ __device__ __forceinline__ void lab_phase(double k, int c, double d, T& re, T& i
     }
 }
 
+// End of a step, shared by the step kernels: the CTA's sums (FP64) go to its
+// slot of the partials (grouped per batch member); the last CTA of the launch
+// reduces each member's partials in a fixed order (one warp per member, so
+// the result does not depend on scheduling), writes M(t), checks it for
+// NaN/Inf and advances the device step counter. red: >= 3 doubles per warp;
+// flag: one shared int.
+template <typename T>
+__device__ __forceinline__ void finish_step(const StepParams<T>& P, long long step, unsigned b, unsigned local,
+                                            unsigned nb_per, double s[3], double* red, int* flag) {
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nthreads / 32;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) red[warp * 3 + c] = s[c];
+    __syncthreads();
+    const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+    if (tid == 0) {
+        double t[3] = {0.0, 0.0, 0.0};
+        for (int w = 0; w < nwarps; ++w)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) t[c] += red[w * 3 + c];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) P.partials[3ull * ((unsigned long long)b * nb_per + local) + c] = t[c];
+        __threadfence();
+        const unsigned prev = atomicAdd(&P.ctl->ticket, 1u);
+        *flag = (prev == nblocks - 1);
+    }
+    __syncthreads();
+    if (!*flag) return;
+    __threadfence();
+    const unsigned nb = P.nbatch > 1 ? (unsigned)P.nbatch : 1u;
+    const long long slot = step - __ldcg(&P.ctl->mt_base);
+    // every thread of the last CTA strides over one member's partials, then a
+    // fixed tree; this tail runs after all other CTAs, on the step's critical path
+    for (unsigned bb = 0; bb < nb; ++bb) {
+        double t[3] = {0.0, 0.0, 0.0};
+        for (unsigned q = tid; q < nb_per; q += nthreads)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) t[c] += __ldcg(&P.partials[3ull * ((unsigned long long)bb * nb_per + q) + c]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t[c] += __shfl_down_sync(0xffffffffu, t[c], o);
+        __syncthreads();  // red is reused
+        if (lane == 0)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) red[warp * 3 + c] = t[c];
+        __syncthreads();
+        if (tid == 0) {
+            double u[3] = {0.0, 0.0, 0.0};
+            for (int w = 0; w < nwarps; ++w)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) u[c] += red[w * 3 + c];
+            if (slot >= 0 && slot < P.mt_cap) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) P.mt[3 * (slot * nb + bb) + c] = u[c];
+            } else {
+                P.ctl->status |= 1;
+            }
+            if (!isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2])) P.ctl->status |= 4;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        P.ctl->ticket = 0;
+        P.ctl->step = step + 1;
+        __threadfence();
+    }
+}
+
 template <typename T, int SCHEME, bool VEL, bool PREC>
 __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ StepParams<T> P) {
     __shared__ T sm[3][TY + 2][TX + 2];
@@ -134,10 +209,16 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const int x = blockIdx.x * TX + tx;
     const int y = blockIdx.y * TY + ty;
-    const int z0 = blockIdx.z * P.zchunk;
+    // blockIdx.z = z-chunk + zsplit * batch member
+    const unsigned nb = P.nbatch > 1 ? (unsigned)P.nbatch : 1u;
+    const int zc = (int)(blockIdx.z % (unsigned)P.zsplit);
+    const unsigned b = blockIdx.z / (unsigned)P.zsplit;
+    const int z0 = zc * P.zchunk;
     const int z1 = min(nz, z0 + P.zchunk);
-    const long long step = P.ctl->step;
-    const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched);
+    const long long step = __ldcg(&P.ctl->step);
+    const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched) * nb + b;
+    const T* in[3] = {P.in[0] + b * P.bstride, P.in[1] + b * P.bstride, P.in[2] + b * P.bstride};
+    T* out[3] = {P.out[0] + b * P.bstride, P.out[1] + b * P.bstride, P.out[2] + b * P.bstride};
     const bool inb = (x < nx) && (y < ny);
     const int xc = min(x, nx - 1), yc = min(y, ny - 1);
     const int pitch = P.pitch;
@@ -186,9 +267,9 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
         const long long oa = (long long)za * plane + col;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            cb[c] = P.in[c][ob];
-            cc[c] = P.in[c][oc];
-            ca[c] = P.in[c][oa];
+            cb[c] = in[c][ob];
+            cc[c] = in[c][oc];
+            ca[c] = in[c][oa];
         }
     }
     T wlo = 0;
@@ -199,7 +280,7 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
         T nxt[3];
         const long long on = (long long)min(z + 2, nz - 1) * plane + col;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) nxt[c] = P.in[c][on];
+        for (int c = 0; c < 3; ++c) nxt[c] = in[c][on];
         const long long oz = (long long)z * plane;
         const uint8_t cd = P.code[(long long)z * cplane + ccol];
         T um = 0, up = 0, vm = 0, vp = 0, whi = 0;
@@ -216,22 +297,22 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
         if (tx == 0) {
             const long long o = oz + (long long)yc * pitch + max(x - 1, 0);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) sm[c][ty + 1][0] = P.in[c][o];
+            for (int c = 0; c < 3; ++c) sm[c][ty + 1][0] = in[c][o];
         }
         if (tx == TX - 1) {
             const long long o = oz + (long long)yc * pitch + min(x + 1, nx - 1);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) sm[c][ty + 1][TX + 1] = P.in[c][o];
+            for (int c = 0; c < 3; ++c) sm[c][ty + 1][TX + 1] = in[c][o];
         }
         if (ty == 0) {
             const long long o = oz + (long long)max(y - 1, 0) * pitch + xc;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) sm[c][0][tx + 1] = P.in[c][o];
+            for (int c = 0; c < 3; ++c) sm[c][0][tx + 1] = in[c][o];
         }
         if (ty == TY - 1) {
             const long long o = oz + (long long)min(y + 1, ny - 1) * pitch + xc;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) sm[c][TY + 1][tx + 1] = P.in[c][o];
+            for (int c = 0; c < 3; ++c) sm[c][TY + 1][tx + 1] = in[c][o];
         }
         __syncthreads();
 
@@ -354,9 +435,9 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
                     accz.add(az);
                 }
             }
-            P.out[0][oz + col] = o0;
-            P.out[1][oz + col] = o1;
-            P.out[2][oz + col] = o2;
+            out[0][oz + col] = o0;
+            out[1][oz + col] = o1;
+            out[2][oz + col] = o2;
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -369,60 +450,9 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
 
     // ---- deterministic M(t) reduction ----
     double s3[3] = {accx.get(), accy.get(), accz.get()};
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s3[c] += __shfl_down_sync(0xffffffffu, s3[c], o);
-    if ((tid & 31) == 0)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) red[tid >> 5][c] = s3[c];
-    __syncthreads();
-    const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
-    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    if (tid == 0) {
-        double t[3] = {0.0, 0.0, 0.0};
-        for (int w = 0; w < NTHREADS / 32; ++w)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) t[c] += red[w][c];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) P.partials[3ull * bid + c] = t[c];
-        __threadfence();
-        const unsigned prev = atomicAdd(&P.ctl->ticket, 1u);
-        last_flag = (prev == nblocks - 1);
-    }
-    __syncthreads();
-    if (!last_flag) return;
-    __threadfence();
-    double t[3] = {0.0, 0.0, 0.0};
-    for (unsigned q = tid; q < nblocks; q += NTHREADS)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) t[c] += __ldcg(&P.partials[3ull * q + c]);
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t[c] += __shfl_down_sync(0xffffffffu, t[c], o);
-    __syncthreads();
-    if ((tid & 31) == 0)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) red[tid >> 5][c] = t[c];
-    __syncthreads();
-    if (tid == 0) {
-        double u[3] = {0.0, 0.0, 0.0};
-        for (int w = 0; w < NTHREADS / 32; ++w)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) u[c] += red[w][c];
-        const long long slot = step - P.ctl->mt_base;
-        if (slot >= 0 && slot < P.mt_cap) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) P.mt[3 * slot + c] = u[c];
-        } else {
-            P.ctl->status |= 1;
-        }
-        if (!isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2])) P.ctl->status |= 4;
-        P.ctl->ticket = 0;
-        P.ctl->step = step + 1;
-        __threadfence();
-    }
+    const unsigned local = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * (unsigned)zc);
+    const unsigned nb_per = gridDim.x * gridDim.y * (unsigned)P.zsplit;
+    finish_step<T>(P, step, b, local, nb_per, s3, &red[0][0], &last_flag);
 }
 
 // sums of a field (bt_measure): FP64 per thread, lab frame for a non-zero k

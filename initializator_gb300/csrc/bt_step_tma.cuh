@@ -87,6 +87,14 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
         "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(sa(bar))
         : "memory");
 }
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3, int c4) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+        "[%7];" ::"r"(sa(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(sa(bar))
+        : "memory");
+}
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
                                             int c2) {
     asm volatile(
@@ -122,13 +130,18 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // so the plane two neighbouring chunks share is read by both at the same
     // moment (both at their start, or both at their end) and the second read
     // hits L2 instead of DRAM.
-    const int zc = blockIdx.x;
+    // blockIdx.x = batch member + nbatch * z-chunk: the members of a q-sweep
+    // run side by side, so the geometry and velocity tiles they share come
+    // from L2 after the first member's DRAM read
+    const unsigned nb = P.nbatch > 1 ? (unsigned)P.nbatch : 1u;
+    const unsigned b = blockIdx.x % nb;
+    const int zc = (int)(blockIdx.x / nb);
     const int x0 = blockIdx.y * TW, y0 = blockIdx.z * TH;
     const int z0 = zc * P.zchunk;
     const int z1 = min(nz, z0 + P.zchunk);
     const int d = (zc & 1) ? -1 : 1;
     const long long step = __ldcg(&P.ctl->step);
-    const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched);
+    const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched) * nb + b;
     const int xb = x0 + QX * lane;  // first of this thread's 4 voxels
     const int y = y0 + w;
 
@@ -138,7 +151,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
         uint64_t* bar = &bars[slot];
         unsigned char* base = smem + slot * STAGE;
         mbar_expect_tx(bar, txbytes);
-        tma_load_4d(base + OFF_STATE, &M.state, bar, x0 - 4, y0 - 1, plane, 0);
+        tma_load_5d(base + OFF_STATE, &M.state, bar, x0 - 4, y0 - 1, plane, 0, (int)b);
         if constexpr (VEL) {
             tma_load_3d(base + OFF_VX, &M.vx, bar, x0, y0, plane);
             tma_load_3d(base + OFF_VY, &M.vy, bar, x0, y0, plane);
@@ -404,7 +417,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
         acc[2].add(sz_);
         if (row_ok && xb < nx) {
-            const long long off = (long long)z * P.plane + (long long)y * P.pitch + xb;
+            const long long off = (long long)b * P.bstride + (long long)z * P.plane + (long long)y * P.pitch + xb;
 #pragma unroll
             for (int c = 0; c < 3; ++c)
                 *reinterpret_cast<float4*>(P.out[c] + off) = make_float4(o[c][0], o[c][1], o[c][2], o[c][3]);
@@ -436,60 +449,9 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // ---- deterministic M(t) reduction (as step_kernel) ----
     {
         double s3[3] = {acc[0].get(), acc[1].get(), acc[2].get()};
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s3[c] += __shfl_down_sync(0xffffffffu, s3[c], o);
-        if (lane == 0)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) red[w * 3 + c] = s3[c];
-        __syncthreads();
-        const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
-        const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        if (tid == 0) {
-            double t[3] = {0.0, 0.0, 0.0};
-            for (int ww = 0; ww < TH; ++ww)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) t[c] += red[ww * 3 + c];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) P.partials[3ull * bid + c] = t[c];
-            __threadfence();
-            const unsigned prev = atomicAdd(&P.ctl->ticket, 1u);
-            s_flags[1] = (prev == nblocks - 1);
-        }
-        __syncthreads();
-        if (!s_flags[1]) return;
-        __threadfence();
-        double t[3] = {0.0, 0.0, 0.0};
-        for (unsigned qb = tid; qb < nblocks; qb += NT)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) t[c] += __ldcg(&P.partials[3ull * qb + c]);
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t[c] += __shfl_down_sync(0xffffffffu, t[c], o);
-        __syncthreads();
-        if (lane == 0)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) red[w * 3 + c] = t[c];
-        __syncthreads();
-        if (tid == 0) {
-            double u[3] = {0.0, 0.0, 0.0};
-            for (int ww = 0; ww < TH; ++ww)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) u[c] += red[ww * 3 + c];
-            const long long slot = step - __ldcg(&P.ctl->mt_base);
-            if (slot >= 0 && slot < P.mt_cap) {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) P.mt[3 * slot + c] = u[c];
-            } else {
-                P.ctl->status |= 1;
-            }
-            if (!isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2])) P.ctl->status |= 4;
-            P.ctl->ticket = 0;
-            P.ctl->step = step + 1;
-            __threadfence();
-        }
+        const unsigned local = (unsigned)zc + (unsigned)P.zsplit * (blockIdx.y + gridDim.y * blockIdx.z);
+        const unsigned nb_per = (unsigned)P.zsplit * gridDim.y * gridDim.z;
+        finish_step<float>(P, step, b, local, nb_per, s3, red, const_cast<int*>(&s_flags[1]));
     }
     return;
 
