@@ -183,6 +183,48 @@ int bt_step_noalloc(const bt_config* cfg, const uint8_t* mask, const void* vx, c
                     const void* mx_in, const void* my_in, const void* mz_in, void* mx_out, void* my_out,
                     void* mz_out, double* sums, void* stream);
 
+/* ---- learned closure: primitives of the 3-D CNN (no reference counterpart) ----
+ * A 4-layer net of 3x3x3 convolutions, 16 -> 16 channels, BF16 operands with
+ * FP32 accumulation on tcgen05 tensor cores, corrects a 2x-coarse, 4x-dt
+ * solve toward the fine one. Activations are channels-last BF16 rows of a
+ * zero-padded grid: row q = [sample][z+1][y+1][x+1] of (nx+2, ny+2, nz+2),
+ * 16 channels (32 bytes) a row, preceded and followed by
+ * bt_conv3d_margin(nx, ny) zero rows; x/out point at the start of the
+ * allocation (margin included). FP32 row arrays (pre, outf) have no margin.
+ * Weights w[27][16 ci][16 co] (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)) are packed
+ * by bt_conv3d_pack_weights into 27*512-byte forward and data-gradient
+ * blocks. All calls are asynchronous on `stream` (a cudaStream_t). */
+typedef struct bt_conv3d_args {
+    int nb, nx, ny, nz;      /* samples and interior grid */
+    int mode;                /* 0: out = GELU(x*w + b) (BF16 rows), pre = x*w + b (FP32 rows)
+                                1: outf = x*w + b (FP32 rows)
+                                2: out = (x*w) * GELU'(pre) (BF16 rows; data gradient)
+                                3: outf = x*w (FP32 rows) */
+    int reserved;
+    const void* x;           /* BF16 padded rows */
+    const void* wpack;       /* 27*512 bytes */
+    const float* bias;       /* 16 floats (modes 0, 1) */
+    void* out;               /* BF16 padded rows (modes 0, 2); halo rows written as zero */
+    float* pre;              /* FP32 rows: written in mode 0 (may be NULL), read in mode 2 */
+    float* outf;             /* FP32 rows (modes 1, 3) */
+    int* status;             /* device int; bit 8 set when a bounded wait gave up */
+} bt_conv3d_args;
+
+long long bt_conv3d_margin(int nx, int ny);
+int bt_conv3d(const bt_conv3d_args* a, void* stream);
+/* grad[28][16][16]: taps 0..26 = dL/dw[t][ci][co]; row 27, ci 0 = dL/db[co].
+ * partial: bt_conv3d_wgrad_scratch(...) floats of device scratch. */
+int bt_conv3d_weight_grad(const void* x, const void* dz, int nb, int nx, int ny, int nz, float* partial,
+                          float* grad, void* stream);
+long long bt_conv3d_wgrad_scratch(int nb, int nx, int ny, int nz);
+int bt_conv3d_pack_weights(const float* w, void* wpack_fwd, void* wpack_dgrad, void* stream);
+/* AdamW on FP32 parameters (step counts from 1). */
+int bt_adamw(float* p, const float* g, float* m, float* v, int n, float lr, float beta1, float beta2, float eps,
+             float weight_decay, int step, void* stream);
+/* One 128x16x16 tensor-core MMA, D[m][n] = sum_k A[m][k] B[n][k] (A, B
+ * row-major BF16, D FP32): checks the descriptor layouts the convolution uses. */
+int bt_umma_selftest(const void* a_bf16, const void* b_bf16, float* d, int* status, void* stream);
+
 /* ---- host-only helpers (no GPU needed) ---- */
 
 /* Parameters of the reference's pulse schedules. */

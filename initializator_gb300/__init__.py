@@ -55,12 +55,22 @@ class SequenceParams(ctypes.Structure):
                 ("gradient_pulse", ctypes.c_double), ("multiple_gradients", ctypes.c_double * 3)]
 
 
+class Conv3dArgs(ctypes.Structure):
+    """bt_conv3d_args of include/bt.h."""
+    _fields_ = [("nb", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("mode", ctypes.c_int), ("reserved", ctypes.c_int), ("x", ctypes.c_void_p),
+                ("wpack", ctypes.c_void_p), ("bias", ctypes.c_void_p), ("out", ctypes.c_void_p),
+                ("pre", ctypes.c_void_p), ("outf", ctypes.c_void_p), ("status", ctypes.c_void_p)]
+
+
 # every symbol include/bt.h declares
 EXPORTS = [
     "bt_create", "bt_destroy", "bt_last_error", "bt_upload_geometry", "bt_set_state", "bt_get_state",
     "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
     "bt_read_mt", "bt_synchronize", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
     "bt_version", "bt_autotune", "bt_step_noalloc",
+    "bt_conv3d_margin", "bt_conv3d", "bt_conv3d_weight_grad", "bt_conv3d_wgrad_scratch", "bt_conv3d_pack_weights",
+    "bt_adamw", "bt_umma_selftest",
 ]
 
 _lib = None
@@ -99,6 +109,14 @@ def lib():
         "bt_version": ([], ctypes.c_char_p),
         "bt_autotune": ([vp, i, ctypes.POINTER(ctypes.c_int)], i),
         "bt_step_noalloc": ([ctypes.POINTER(Config), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
+        "bt_conv3d_margin": ([i, i], ll),
+        "bt_conv3d": ([ctypes.POINTER(Conv3dArgs), vp], i),
+        "bt_conv3d_weight_grad": ([vp, vp, i, i, i, i, vp, vp, vp], i),
+        "bt_conv3d_wgrad_scratch": ([i, i, i, i], ll),
+        "bt_conv3d_pack_weights": ([vp, vp, vp, vp], i),
+        "bt_adamw": ([vp, vp, vp, vp, i, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                      ctypes.c_float, i, vp], i),
+        "bt_umma_selftest": ([vp, vp, vp, vp, vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(l, name)

@@ -7,6 +7,7 @@ Translation units are compiled in parallel with nvcc (one -gencode, no cmake):
   multiply-add contraction changes the reference's rounding
 * ``bt_api.cu``      — host runtime behind include/bt.h
 * ``bt_noalloc.cu``   — the allocation-free single-step entry point
+* ``bt_closure.cu``   — tcgen05 implicit-GEMM 3-D convolution of the learned closure
 * ``bt_schedule.cpp`` — host replay of the reference's pulse schedules
 * ``host/NmrRelaxationSolve.cpp`` + ``host/nmr_io.cpp`` — the drop-in C++ class
   (linked into the same library, and into the ``nmr_exe`` program)
@@ -35,6 +36,7 @@ UNITS = [
     ("bt_step_f64.cu", ARCH + ["-fmad=false"]),
     ("bt_api.cu", ARCH),
     ("bt_noalloc.cu", ARCH),
+    ("bt_closure.cu", ARCH),
     ("bt_schedule.cpp", []),
 ]
 HOST_UNITS = [os.path.join("host", "NmrRelaxationSolve.cpp"), os.path.join("host", "nmr_io.cpp")]
