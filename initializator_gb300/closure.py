@@ -90,3 +90,98 @@ def weight_grad(layout: PaddedRows, x, dz, scratch=None):
     if rc:
         raise BtError(rc, "bt_conv3d_weight_grad")
     return grad[:TAPS], grad[TAPS, 0], scratch
+
+
+class Net:
+    """4 conv layers, 16 -> 16 channels, GELU after the first three. FP32
+    master parameters in one flat buffer (for AdamW), packed BF16 copies for
+    the kernels. The last layer starts at zero, so an untrained net leaves the
+    coarse solve unchanged."""
+
+    NW = 4 * TAPS * CH * CH
+    NP = NW + 4 * CH
+
+    def __init__(self, device="cuda", seed=0, scale=1.0, zero_last=True):
+        import torch
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        self.device = device
+        self.flat = torch.zeros(self.NP, dtype=torch.float32)
+        w = self.flat[:self.NW].view(4, TAPS, CH, CH)
+        for i in range(4):
+            w[i] = torch.randn((TAPS, CH, CH), generator=g) * (scale / np.sqrt(TAPS * CH))
+        if zero_last:
+            w[3].zero_()
+        self.flat = self.flat.to(device)
+        self.grad = torch.zeros_like(self.flat)
+        self.m = torch.zeros_like(self.flat)
+        self.v = torch.zeros_like(self.flat)
+        self.step_count = 0
+        self.status = torch.zeros(1, dtype=torch.int32, device=device)
+        self.repack()
+
+    def w(self, i):
+        return self.flat[:self.NW].view(4, TAPS, CH, CH)[i]
+
+    def b(self, i):
+        return self.flat[self.NW:].view(4, CH)[i]
+
+    def repack(self):
+        self.packed = [pack_weights(self.w(i)) for i in range(4)]
+
+    def forward(self, layout: PaddedRows, x):
+        """x: BF16 padded rows -> FP32 output rows (16 channels), with the
+        activations and pre-activations kept for backward."""
+        import torch
+        acts, pres = [x], []
+        a = x
+        for i in range(3):
+            out = layout.empty(self.device)
+            pre = torch.empty((layout.rows, CH), dtype=torch.float32, device=self.device)
+            conv3d(layout, a, self.packed[i][0], 0, bias=self.b(i), out=out, pre=pre, status=self.status)
+            acts.append(out)
+            pres.append(pre)
+            a = out
+        y = torch.empty((layout.rows, CH), dtype=torch.float32, device=self.device)
+        conv3d(layout, a, self.packed[3][0], 1, bias=self.b(3), outf=y, status=self.status)
+        self._cache = (acts, pres)
+        return y
+
+    def backward(self, layout: PaddedRows, dy):
+        """dy: FP32 rows (zero on the halo) = dL/dy. Fills self.grad."""
+        acts, pres = self._cache
+        g = layout.empty(self.device)
+        g[layout.margin:layout.margin + layout.rows] = dy.to(g.dtype)
+        gw = self.grad[:self.NW].view(4, TAPS, CH, CH)
+        gb = self.grad[self.NW:].view(4, CH)
+        scratch = None
+        for i in range(3, -1, -1):
+            gwi, gbi, scratch = weight_grad(layout, acts[i], g, scratch)
+            gw[i] = gwi
+            gb[i] = gbi
+            if i > 0:
+                nxt = layout.empty(self.device)
+                conv3d(layout, g, self.packed[i][1], 2, out=nxt, pre=pres[i - 1], status=self.status)
+                g = nxt
+
+    def adamw(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.01):
+        import torch
+        self.step_count += 1
+        rc = lib().bt_adamw(_ptr(self.flat), _ptr(self.grad), _ptr(self.m), _ptr(self.v), self.NP,
+                            ctypes.c_float(lr), ctypes.c_float(beta1), ctypes.c_float(beta2), ctypes.c_float(eps),
+                            ctypes.c_float(weight_decay), self.step_count,
+                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if rc:
+            raise BtError(rc, "bt_adamw")
+        self.repack()
+
+    def check_status(self):
+        if int(self.status.item()) != 0:
+            raise BtError(-6, "a bounded wait in the convolution kernel gave up")
+
+    def state_dict(self):
+        return {"flat": self.flat.detach().cpu().numpy()}
+
+    def load_state_dict(self, d):
+        import torch
+        self.flat.copy_(torch.as_tensor(d["flat"], device=self.device))
+        self.repack()
