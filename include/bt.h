@@ -149,6 +149,14 @@ int bt_measure(bt_handle* h, double* sums3);
  * *best_zsplit (may be NULL) receives the chosen split. */
 int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit);
 
+/* Device pointers of the current field of batch member `member` (no
+ * reference counterpart: the learned closure corrects the field in place).
+ * Layout [nz][ny][pitch] in the handle's precision; for the KSPACE scheme the
+ * transverse components are in the frame of k at the current step. Valid until
+ * the next bt_run / bt_set_state / bt_get_state on the handle; work on them in
+ * the handle's stream order (bt_stream). */
+int bt_field_device(bt_handle* h, int member, void** mx, void** my, void** mz, int* pitch);
+
 /* Number of kernel launches this handle has issued (a launch inside a replayed
  * CUDA graph counts once per replay). */
 long long bt_launch_count(const bt_handle* h);

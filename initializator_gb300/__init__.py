@@ -70,7 +70,7 @@ EXPORTS = [
     "bt_read_mt", "bt_synchronize", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
     "bt_version", "bt_autotune", "bt_step_noalloc",
     "bt_conv3d_margin", "bt_conv3d", "bt_conv3d_weight_grad", "bt_conv3d_wgrad_scratch", "bt_conv3d_pack_weights",
-    "bt_adamw", "bt_umma_selftest",
+    "bt_adamw", "bt_umma_selftest", "bt_field_device",
 ]
 
 _lib = None
@@ -117,6 +117,8 @@ def lib():
         "bt_adamw": ([vp, vp, vp, vp, i, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                       ctypes.c_float, i, vp], i),
         "bt_umma_selftest": ([vp, vp, vp, vp, vp], i),
+        "bt_field_device": ([vp, i, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                             ctypes.POINTER(ctypes.c_int)], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(l, name)
@@ -284,9 +286,38 @@ class Solver:
         self._check(self._l.bt_autotune(self._h, int(trial_steps), ctypes.byref(best)), "autotune")
         return best.value
 
+    def field_views(self, member=0):
+        """torch views (3 x [nz][ny][nx], strided by the pitch) of the current
+        field on the device (k frame for KSPACE); valid until the next run."""
+        import torch
+        ptrs = [ctypes.c_void_p() for _ in range(3)]
+        pitch = ctypes.c_int(0)
+        self._check(self._l.bt_field_device(self._h, member, *[ctypes.byref(p) for p in ptrs], ctypes.byref(pitch)),
+                    "field_device")
+        dt = torch.float64 if self.cfg.precision == BT_F64 else torch.float32
+        nz, ny, nx = self.shape
+        esz = 8 if dt == torch.float64 else 4
+        views = []
+        for p in ptrs:
+            flat = _cuda_tensor_from_ptr(p.value, nz * ny * pitch.value, dt)
+            views.append(flat.view(nz, ny, pitch.value)[:, :, :nx])
+        return views
+
     @property
     def launches(self):
         return int(self._l.bt_launch_count(self._h))
+
+
+def _cuda_tensor_from_ptr(ptr, n, dtype):
+    """A torch tensor over device memory owned by the library (no copy)."""
+    import torch
+    class _Wrap:
+        pass
+    w = _Wrap()
+    typestr = {torch.float32: "<f4", torch.float64: "<f8"}[dtype]
+    w.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 3,
+                                  "strides": None}
+    return torch.as_tensor(w, device="cuda")
 
 
 def kspace_waveform_pgse(nsteps, dt, g_amp, delta, Delta, axis=(0.0, 0.0, 1.0)):

@@ -802,6 +802,16 @@ int bt_measure(bt_handle* h, double* sums3) {
 
 long long bt_launch_count(const bt_handle* h) { return h ? h->launches : -1; }
 
+int bt_field_device(bt_handle* h, int member, void** mx, void** my, void** mz, int* pitch) {
+    if (!h || member < 0 || member >= h->nb || !mx || !my || !mz || !pitch) return fail(h, BT_E_ARG, "bad field query");
+    const size_t off = (size_t)member * 3 * h->comp * h->esz;
+    *mx = (char*)h->state[h->cur][0] + off;
+    *my = (char*)h->state[h->cur][1] + off;
+    *mz = (char*)h->state[h->cur][2] + off;
+    *pitch = h->pitch;
+    return BT_OK;
+}
+
 int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
     if (!h || trial_steps <= 0) return fail(h, BT_E_ARG, "bad autotune arguments");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
