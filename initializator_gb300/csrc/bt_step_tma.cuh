@@ -6,8 +6,11 @@
 //   * each z-plane of the tile (the three field components with a one-voxel
 //     x/y halo, face velocities, geometry code) is fetched by one thread with
 //     cp.async.bulk.tensor into a 3-slot shared-memory ring, completion
-//     tracked by one mbarrier per slot (expect_tx), so two planes are in
-//     flight while the CTA computes the current one;
+//     tracked by one "full" mbarrier per slot (expect_tx), so two planes are
+//     in flight while the CTA computes the current one; each warp releases a
+//     slot through the slot's "empty" mbarrier (one arrival per warp) and only
+//     the producing thread waits for it, so the warps of a CTA drift up to two
+//     planes apart instead of meeting at a CTA barrier every plane;
 //   * each thread computes 4 consecutive voxels along x: 128-bit shared
 //     loads, 128-bit global stores; the voxel's own z-column (below / current
 //     / above) rolls through registers;
@@ -18,8 +21,10 @@
 //     keeps the reference's exact operation order in step_kernel.
 // Out-of-range TMA boxes (halo beyond the domain, plane -1 or nz) are
 // zero-filled and never used as data.
-// Every mbarrier wait is bounded; on timeout the CTA records status bit 8,
-// drains its copies (bounded) and returns without touching the step counter.
+// Every mbarrier wait is bounded; a wait that gives up raises the CTA's
+// failure flag, which ends the other warps' waits too; after the march the
+// CTA then records status bit 8, drains its copies (bounded) and returns
+// without touching the step counter.
 #pragma once
 #include "bt_step.cuh"
 
@@ -59,6 +64,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sa(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(bar)), "r"(bytes) : "memory");
 }
@@ -72,12 +80,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "r"(sa(bar)), "r"(parity)
         : "memory");
     return ok != 0;
-}
-// bounded wait: false after WAIT_LIMIT polls
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < WAIT_LIMIT; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
 }
 __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
                                             int c3) {
@@ -115,10 +117,12 @@ __global__ void __launch_bounds__(tma::NT, 2)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem = smem_raw + ((128u - (sa(smem_raw) & 127u)) & 127u);
     // aux layout (bytes from OFF_AUX): code table 0..4095 (128 rows x 8 floats),
-    // ey 4096..4159, barriers 4160..4183, flags 4224..4231, red 4288..4479, ez 4608..
+    // ey 4096..4159, full barriers 4160..4183, empty barriers 4184..4207,
+    // flags 4224..4231, red 4288..4479, ez 4608..
     float4* s_tab = reinterpret_cast<float4*>(smem + OFF_AUX);
     float2* s_ey = reinterpret_cast<float2*>(smem + OFF_AUX + 4096);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_AUX + 4160);
+    uint64_t* empties = bars + NSTAGE;
     int* s_flags = reinterpret_cast<int*>(smem + OFF_AUX + 4224);
     double* red = reinterpret_cast<double*>(smem + OFF_AUX + 4288);
     float2* s_ez = reinterpret_cast<float2*>(smem + OFF_AUX + 4608);
@@ -168,7 +172,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // plane q lands in slot q % NSTAGE as that slot's (q / NSTAGE)-th phase
     int n_issued = 0;  // planes issued so far (thread 0), always in plane order
     if (tid == 0) {
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < NSTAGE; ++s) {
+            mbar_init(&bars[s], 1);
+            mbar_init(&empties[s], TH);
+        }
         fence_mbar_init();
         s_flags[0] = 0;
         for (int q = 0; q < NSTAGE && q < nplanes; ++q) {
@@ -244,38 +251,64 @@ __global__ void __launch_bounds__(tma::NT, 2)
             dst[0] = v.x; dst[1] = v.y; dst[2] = v.z; dst[3] = v.w;
         }
     };
-    bool ok = true;
-    auto wait_slot = [&](int q) {
-        const int slot = q % NSTAGE;
-        if (!mbar_wait(&bars[slot], (uint32_t)(q / NSTAGE) & 1u)) ok = false;
-        return slot;
+    // s_flags[0] is the CTA's failure flag (volatile: polled inside waits)
+    volatile int* vflag = s_flags;
+    // warp-uniform bounded wait for plane q's copy; false when it gave up or
+    // another thread of the CTA raised the failure flag
+    auto wait_full = [&](int q) -> bool {
+        const uint32_t par = (uint32_t)(q / NSTAGE) & 1u;
+        for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+            if (__all_sync(0xffffffffu, mbar_try_wait(&bars[q % NSTAGE], par))) return true;
+            if (__any_sync(0xffffffffu, vflag[0] != 0)) return false;
+        }
+        if (lane == 0) vflag[0] = 1;
+        return false;
+    };
+    // a warp is done with plane q's slot
+    auto release = [&](int q) {
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empties[q % NSTAGE]);
+    };
+    // producer (thread 0): plane p into slot p % NSTAGE once every warp has
+    // released plane p - NSTAGE from it (bounded; raises the flag on timeout)
+    auto refill = [&](int p) {
+        const uint32_t par = (uint32_t)((p - NSTAGE) / NSTAGE) & 1u;
+        for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+            if (mbar_try_wait(&empties[p % NSTAGE], par)) {
+                fence_proxy_async();
+                issue(p % NSTAGE, plane_of(p));
+                n_issued++;
+                return;
+            }
+            if (vflag[0]) return;
+        }
+        vflag[0] = 1;
     };
 
     // prologue: the ghost-side plane (q = 0) and the first plane (q = 1)
-    if (!empty) {
-        const int s0 = wait_slot(0);
-        own(s0, prv);
-        own_vz(s0, vzp);
-        const int s1 = wait_slot(1);
-        own(s1, cur);
-        own_vz(s1, vzc);
-        if (!ok) s_flags[0] = 1;
-        __syncthreads();
-        if (s_flags[0]) goto abort;
-        if (tid == 0 && nplanes > NSTAGE) {
-            fence_proxy_async();
-            issue(s0, plane_of(NSTAGE));
-            n_issued++;
+    bool live = !empty;
+    if (live) {
+        live = wait_full(0);
+        if (live) {
+            own(0, prv);
+            own_vz(0, vzp);
+            live = wait_full(1);
+        }
+        if (live) {
+            own(1, cur);
+            own_vz(1, vzc);
+            release(0);
+            if (tid == 0 && nplanes > NSTAGE) refill(NSTAGE);
         }
     }
 
-    for (int q = 1; q + 1 < nplanes; ++q) {
+    for (int q = 1; live && q + 1 < nplanes; ++q) {
         const int z = plane_of(q);
         const int sc = q % NSTAGE;
-        const int sn = wait_slot(q + 1);
+        if (!wait_full(q + 1)) break;
+        const int sn = (q + 1) % NSTAGE;
         own(sn, nxt);
         own_vz(sn, vzn);
-        if (!ok) s_flags[0] = 1;
         // one instance of the plane body per marching direction, so that
         // below / above and the upper face velocity bind to fixed registers
         auto body = [&](const float(&bel)[3][QX], const float(&abv)[3][QX], const float(&whi)[QX]) {
@@ -425,13 +458,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
         };
         if (d > 0) body(prv, nxt, vzn);
         else body(nxt, prv, vzp);
-        __syncthreads();  // every thread is done with slot sc and with the previous one
-        if (s_flags[0]) goto abort;
-        if (tid == 0 && q + NSTAGE < nplanes) {
-            fence_proxy_async();
-            issue(sc, plane_of(q + NSTAGE));
-            n_issued++;
-        }
+        release(q);
+        if (tid == 0 && q + NSTAGE < nplanes) refill(q + NSTAGE);
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -445,6 +473,11 @@ __global__ void __launch_bounds__(tma::NT, 2)
             vzc[i] = vzn[i];
         }
     }
+
+    // the flag is only written inside the march: after this barrier every
+    // thread sees its final value, so the branch below is CTA-uniform
+    __syncthreads();
+    if (vflag[0]) goto abort;
 
     // ---- deterministic M(t) reduction (as step_kernel) ----
     {
