@@ -119,6 +119,72 @@ def run_qsweep(args, lr):
                          "bytes_per_voxel_step": 24 + 13 / QBATCH}}
 
 
+RAGGED_N = 48               # C3b: 48 independent sphere packs
+RAGGED_STEPS = 3000
+
+
+def ragged_workload(seed=SEED + 11):
+    """C3b: 48 sphere packs, each edge uniform in [48, 192] voxels, solid
+    fraction uniform in [0.3, 0.5], sphere radius 6; no flow."""
+    from initializator_gb300 import geometry
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(RAGGED_N):
+        shape = tuple(int(e) for e in rng.integers(48, 193, size=3))
+        out.append(geometry.sphere_pack(shape, 6.0, float(rng.uniform(0.3, 0.5)), seed=seed + 100 + i))
+    return out
+
+
+def run_ragged(args, lr):
+    """C3b ragged batch: 48 independent samples of different sizes, PGSE as
+    C2 (no flow), 3000 time steps each, advanced together by run_many (each
+    handle's captured step graphs interleaved on its own stream) and, for
+    comparison, one sample after another as a one-sample-per-process run
+    would. Algorithmic bytes per voxel-step: 25."""
+    import torch
+
+    import initializator_gb300 as bt
+    masks = ragged_workload()
+    kw, wave, rf = physics(RAGGED_STEPS + 64)
+    kw = dict(kw, velocity=0)
+    solvers = []
+    for m in masks:
+        s = bt.Solver(bt.make_config(m.shape, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, **kw))
+        s.upload_geometry(m)
+        s.set_schedule(rf, grad_wave=wave)
+        st0 = np.zeros((3,) + m.shape)
+        st0[0] = m
+        s.set_state(st0)
+        solvers.append(s)
+    nvox = sum(int(np.prod(m.shape)) for m in masks)
+    # warm-up: graph capture and first touch (64 steps), then back to step 0
+    bt.run_many(solvers, 64)
+    for s in solvers:
+        s.set_step(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mts = bt.run_many(solvers, RAGGED_STEPS)
+    torch.cuda.synchronize()
+    t_many = time.perf_counter() - t0
+    finite = all(bool(np.all(np.isfinite(m))) for m in mts)
+    for s in solvers:
+        s.set_step(0)
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.run(RAGGED_STEPS)
+    t_seq = time.perf_counter() - t0
+    for s in solvers:
+        s.close()
+    peak, peak_kind = hbm_peak()
+    v_many = nvox * RAGGED_STEPS / t_many
+    return {"workload": "C3b: 48 sphere packs, edges U[48,192], phi_s U[0.3,0.5], PGSE z G=0.1 T/m, no flow, FP32, "
+                        "3000 steps", "voxels": nvox, "value": v_many, "unit": UNIT,
+            "seconds": t_many, "sequential_value": nvox * RAGGED_STEPS / t_seq, "sequential_seconds": t_seq,
+            "finite": finite,
+            "roofline": {"bound": "hbm", "achieved": v_many * 25 / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": v_many * 25 / 1e9 / peak, "peak_kind": peak_kind, "bytes_per_voxel_step": 25}}
+
+
 def physics(total_steps):
     import initializator_gb300 as bt
     from initializator_gb300 import geometry
@@ -352,6 +418,7 @@ def run_ours(args):
     e2e = nvox * S * args.steps * w / e2e_s
     s.close()
     qsweep = None if args.no_qsweep else run_qsweep(args, lr)
+    ragged = None if args.no_ragged else run_ragged(args, lr)
 
     out = None
     if r == 0:
@@ -373,6 +440,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "clocks": clk,
             "qsweep": qsweep,
+            "ragged": ragged,
         }
         print(json.dumps(out))
     if w > 1:
@@ -389,6 +457,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-qsweep", action="store_true", help="skip the batched 32-gradient q-sweep (C3a) leg")
+    ap.add_argument("--no-ragged", action="store_true", help="skip the 48-sample ragged batch (C3b) leg")
     ap.add_argument("--zsplit", type=int, default=0, help="fixed z-chunking of the fast path (skips the autotuner)")
     ap.add_argument("--profile", action="store_true",
                     help="device-resident phase only (for ncu captures); prints no bench line")

@@ -135,6 +135,14 @@ int bt_run(bt_handle* h, long long nsteps, double* mt_out);
 /* Asynchronous form for timing and pipelines: M(t) stays in the handle's
  * device buffer; bt_read_mt copies the sums of the last bt_run_async. */
 int bt_run_async(bt_handle* h, long long nsteps);
+
+/* Ragged batch: advance n independent handles (each with its own grid size,
+ * geometry and schedule) by nsteps each, asynchronously. Launches are
+ * interleaved round robin, one captured graph of steps per handle per round,
+ * so small grids on the handles' separate streams run side by side on the
+ * GPU. Read each handle's M(t) with bt_read_mt. No reference counterpart: the
+ * reference runs one sample per process (main.cpp:34-36). */
+int bt_run_many(bt_handle* const* hs, int n, long long nsteps);
 int bt_read_mt(bt_handle* h, double* mt_out, long long nsteps);
 int bt_synchronize(bt_handle* h);
 /* The handle's stream as a cudaStream_t (void* keeps this header CUDA-free). */

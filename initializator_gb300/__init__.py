@@ -67,7 +67,7 @@ class Conv3dArgs(ctypes.Structure):
 EXPORTS = [
     "bt_create", "bt_destroy", "bt_last_error", "bt_upload_geometry", "bt_set_state", "bt_get_state",
     "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
-    "bt_read_mt", "bt_synchronize", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
+    "bt_run_many", "bt_read_mt", "bt_synchronize", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
     "bt_version", "bt_autotune", "bt_step_noalloc",
     "bt_conv3d_margin", "bt_conv3d", "bt_conv3d_weight_grad", "bt_conv3d_wgrad_scratch", "bt_conv3d_pack_weights",
     "bt_adamw", "bt_umma_selftest", "bt_field_device",
@@ -99,6 +99,7 @@ def lib():
         "bt_set_step": ([vp, ll], i),
         "bt_run": ([vp, ll, dp], i),
         "bt_run_async": ([vp, ll], i),
+        "bt_run_many": ([ctypes.POINTER(vp), i, ll], i),
         "bt_read_mt": ([vp, dp, ll], i),
         "bt_synchronize": ([vp], i),
         "bt_stream": ([vp], vp),
@@ -275,6 +276,15 @@ class Solver:
     def stream_ptr(self):
         return self._l.bt_stream(self._h)
 
+    def torch_stream(self):
+        """The handle's own (non-blocking) CUDA stream as a torch stream: torch
+        work on field_views() issued under it is ordered with the handle's
+        launches without a host synchronisation."""
+        import torch
+        if getattr(self, "_ts", None) is None:
+            self._ts = torch.cuda.ExternalStream(self.stream_ptr)
+        return self._ts
+
     def measure(self):
         out = np.zeros((self.batch, 3))
         self._check(self._l.bt_measure(self._h, _dp(out)), "measure")
@@ -306,6 +316,19 @@ class Solver:
     @property
     def launches(self):
         return int(self._l.bt_launch_count(self._h))
+
+
+def run_many(solvers, nsteps):
+    """Ragged batch: advance independent solvers (any grid sizes) by nsteps
+    each, their launches interleaved on their own streams; returns each
+    solver's M(t) ((nsteps, 3) per solver, or (nsteps, B, 3))."""
+    solvers = list(solvers)
+    arr = (ctypes.c_void_p * max(1, len(solvers)))(*[s._h.value for s in solvers])
+    rc = lib().bt_run_many(arr, len(solvers), int(nsteps))
+    if rc:
+        msgs = "; ".join(s._l.bt_last_error(s._h).decode() for s in solvers if s._l.bt_last_error(s._h))
+        raise BtError(rc, f"run_many: {msgs}")
+    return [s.read_mt(nsteps) for s in solvers]
 
 
 def _cuda_tensor_from_ptr(ptr, n, dtype):

@@ -694,7 +694,8 @@ int bt_set_step(bt_handle* h, long long step) {
     return BT_OK;
 }
 
-int bt_run_async(bt_handle* h, long long nsteps) {
+// checks and device control block for a run of nsteps from the current step
+int run_begin(bt_handle* h, long long nsteps) {
     if (!h || nsteps < 0) return fail(h, BT_E_ARG, "bad step count");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
     const bt_config& c = h->cfg;
@@ -710,20 +711,26 @@ int bt_run_async(bt_handle* h, long long nsteps) {
     h->ctl_h->ticket = 0;
     h->ctl_h->status = 0;
     CK(h, cudaMemcpyAsync(h->ctl_d, h->ctl_h, sizeof(bt::Ctl), cudaMemcpyHostToDevice, h->stream));
-    long long s = h->step;
-    const long long end = h->step + nsteps;
-    while (s < end) {
-        bool clean = end - s >= GRAPH_STEPS;
-        for (long long q = s; clean && q < s + GRAPH_STEPS; ++q) clean = !step_has_pulse(h, q);
+    h->last_run = nsteps;
+    return BT_OK;
+}
+
+// enqueue steps [*s, min(end, *s + limit)) on the handle's stream: runs of
+// GRAPH_STEPS pulse-free steps from a graph captured once per input side,
+// single launches otherwise
+int run_advance(bt_handle* h, long long* s, long long end, long long limit) {
+    const long long stop = std::min(end, *s + limit);
+    while (*s < stop) {
+        bool clean = stop - *s >= GRAPH_STEPS;
+        for (long long q = *s; clean && q < *s + GRAPH_STEPS; ++q) clean = !step_has_pulse(h, q);
         if (clean) {
-            // a graph of GRAPH_STEPS pulse-free launches, captured once per input side
             cudaGraphExec_t& g = h->graph[h->cur];
             if (!g) {
                 cudaGraph_t graph;
                 CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
                 cudaError_t e = cudaSuccess;
                 const long long before = h->launches;
-                for (int q = 0; q < GRAPH_STEPS && e == cudaSuccess; ++q) e = launch_one(h, (h->cur + q) & 1, s + q);
+                for (int q = 0; q < GRAPH_STEPS && e == cudaSuccess; ++q) e = launch_one(h, (h->cur + q) & 1, *s + q);
                 h->launches = before;
                 cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
                 CK(h, e);
@@ -734,15 +741,48 @@ int bt_run_async(bt_handle* h, long long nsteps) {
             }
             CK(h, cudaGraphLaunch(g, h->stream));
             h->launches += GRAPH_STEPS;
-            s += GRAPH_STEPS;
+            *s += GRAPH_STEPS;
         } else {
-            CK(h, launch_one(h, h->cur, s));
+            CK(h, launch_one(h, h->cur, *s));
             h->cur ^= 1;
-            s += 1;
+            *s += 1;
         }
     }
-    h->step = end;
-    h->last_run = nsteps;
+    h->step = *s;
+    return BT_OK;
+}
+
+int bt_run_async(bt_handle* h, long long nsteps) {
+    int rc = run_begin(h, nsteps);
+    if (rc) return rc;
+    long long s = h->step;
+    return run_advance(h, &s, h->step + nsteps, nsteps);
+}
+
+int bt_run_many(bt_handle* const* hs, int n, long long nsteps) {
+    if (!hs || n < 0 || nsteps < 0) return BT_E_ARG;
+    for (int i = 0; i < n; ++i)
+        if (!hs[i]) return BT_E_ARG;
+    for (int i = 0; i < n; ++i) {
+        int rc = run_begin(hs[i], nsteps);
+        if (rc) return rc;
+    }
+    std::vector<long long> pos(n), end(n);
+    for (int i = 0; i < n; ++i) {
+        pos[i] = hs[i]->step;
+        end[i] = hs[i]->step + nsteps;
+    }
+    // round robin, one graph's worth of steps per handle per round, so that
+    // handles whose streams share a hardware queue still interleave
+    for (bool more = true; more;) {
+        more = false;
+        for (int i = 0; i < n; ++i) {
+            if (pos[i] >= end[i]) continue;
+            int rc = run_advance(hs[i], &pos[i], end[i], GRAPH_STEPS);
+            if (rc) return rc;
+            more = more || pos[i] < end[i];
+        }
+    }
     return BT_OK;
 }
 

@@ -302,3 +302,40 @@ def test_batched_q_sweep_matches_single_fields(precision, btlib):
         assert np.array_equal(st[b], st1), b
         assert rel_err(mt[:, b], mt1) <= 1e-12, b
         assert rel_err(m_end[b], mt1[-1]) <= 1e-6, b
+
+
+def test_ragged_batch_matches_single_runs(btlib):
+    """run_many over handles of different sizes, precisions, schemes and
+    schedules (graph chunks interleaved on separate streams) against each
+    handle run alone: fields and M(t) bit-identical; one member also against
+    the oracle's physics mode."""
+    import initializator_gb300 as bt
+    import oracle
+    specs = [((20, 18, 36), 5, bt.BT_F32), ((12, 10, 16), 6, bt.BT_F64), ((24, 16, 40), 7, bt.BT_F32),
+             ((8, 8, 8), 8, bt.BT_F32)]
+    n = 100  # three graph chunks of 32 steps plus single launches around the pulses
+
+    def make(shape, seed, prec):
+        mask, vel, st0, kw, wave, rf, nn = _kspace_case(shape, seed)
+        s = bt.Solver(bt.make_config(shape, precision=prec, scheme=bt.BT_SCHEME_KSPACE, **kw))
+        s.upload_geometry(mask, vel)
+        s.set_schedule(rf, grad_wave=wave)
+        s.set_state(st0)
+        return s, (mask, vel, st0, kw, wave, rf)
+
+    many = [make(*sp) for sp in specs]
+    mts = bt.run_many([s for s, _ in many], n)
+    states = [s.get_state() for s, _ in many]
+    for (s, _), sp, mt, st in zip(many, specs, mts, states):
+        s.close()
+        one, _ = make(*sp)
+        with one:
+            mt1 = one.run(n)
+            st1 = one.get_state()
+        assert np.array_equal(st, st1), sp
+        assert np.array_equal(mt, mt1), sp
+    mask, vel, st0, kw, wave, rf = many[1][1]
+    p = oracle.make_params(specs[1][0], main_field=(0, 0, 1), vector_mult=2, **kw)
+    ref, ref_mt = oracle.run(p, mask, st0, n, vel=vel, pulses=rf, grad_wave=wave)
+    assert rel_err(states[1], ref) <= KS64_TOL
+    assert rel_err(mts[1], ref_mt) <= KS64_TOL
