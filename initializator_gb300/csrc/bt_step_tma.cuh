@@ -52,7 +52,16 @@ constexpr int OFF_CODE = OFF_VZ + SZ_VZ;                    // 29312
 constexpr int SZ_CODE = TH * TW;                            // 1024
 constexpr int STAGE = OFF_CODE + SZ_CODE;                   // 30336
 constexpr int OFF_AUX = NSTAGE * STAGE;                     // tables, barriers, reduction
-constexpr int SMEM = OFF_AUX + 4608 + 8 * ZCHUNK_MAX + 128;  // + 128 for the base alignment
+// aux layout (bytes from OFF_AUX)
+constexpr int TAB_ROW = 12;                  // floats per code-table row: 48 B, so 8 distinct rows hit 8 bank groups
+constexpr int AUX_TAB = 0;                   // 128 rows: 6 face weights, dt/T1, dt/T2, 4 unused
+constexpr int AUX_EY = AUX_TAB + 128 * TAB_ROW * 4;  // 6144: exp(-i k_y y), TH float2
+constexpr int AUX_BARS = AUX_EY + 64;        // full[NSTAGE], empty[NSTAGE]
+constexpr int AUX_FLAGS = AUX_BARS + 64;
+constexpr int AUX_RED = AUX_FLAGS + 128;     // 8 warps x 3 doubles
+constexpr int AUX_EX = AUX_RED + 256;        // exp(-i k_x x), TW float2
+constexpr int AUX_EZ = AUX_EX + 8 * TW;      // exp(-i k_z z), up to ZCHUNK_MAX float2
+constexpr int SMEM = OFF_AUX + AUX_EZ + 8 * ZCHUNK_MAX + 128;  // + 128 for the base alignment
 static_assert(OFF_VX % 128 == 0 && OFF_VY % 128 == 0 && OFF_VZ % 128 == 0 && OFF_CODE % 128 == 0, "align");
 static_assert(STAGE % 128 == 0, "align");
 constexpr uint32_t WAIT_LIMIT = 1u << 20;  // polls; a healthy copy lands in microseconds
@@ -116,16 +125,14 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // shared-memory base explicitly (the launch reserves 128 spare bytes)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem = smem_raw + ((128u - (sa(smem_raw) & 127u)) & 127u);
-    // aux layout (bytes from OFF_AUX): code table 0..4095 (128 rows x 8 floats),
-    // ey 4096..4159, full barriers 4160..4183, empty barriers 4184..4207,
-    // flags 4224..4231, red 4288..4479, ez 4608..
-    float4* s_tab = reinterpret_cast<float4*>(smem + OFF_AUX);
-    float2* s_ey = reinterpret_cast<float2*>(smem + OFF_AUX + 4096);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_AUX + 4160);
+    float4* s_tab = reinterpret_cast<float4*>(smem + OFF_AUX + AUX_TAB);
+    float2* s_ey = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_EY);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_AUX + AUX_BARS);
     uint64_t* empties = bars + NSTAGE;
-    int* s_flags = reinterpret_cast<int*>(smem + OFF_AUX + 4224);
-    double* red = reinterpret_cast<double*>(smem + OFF_AUX + 4288);
-    float2* s_ez = reinterpret_cast<float2*>(smem + OFF_AUX + 4608);
+    int* s_flags = reinterpret_cast<int*>(smem + OFF_AUX + AUX_FLAGS);
+    double* red = reinterpret_cast<double*>(smem + OFF_AUX + AUX_RED);
+    float2* s_ex = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_EX);
+    float2* s_ez = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_EZ);
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, w = tid >> 5;
@@ -191,20 +198,30 @@ __global__ void __launch_bounds__(tma::NT, 2)
         const float dm = (pore && P.diffusion) ? 1.f : 0.f;
         const float kx = P.hxx * P.dpp, ky = P.hyy * P.dpp, kz = P.hzz * P.dpp;
         const float sx = P.hxx * P.dps, sy = P.hyy * P.dps, sz = P.hzz * P.dps;
-        s_tab[2 * tid] = make_float4(dm * ((f & 1) ? sx : kx), dm * ((f & 2) ? sx : kx), dm * ((f & 4) ? sy : ky),
+        s_tab[3 * tid] = make_float4(dm * ((f & 1) ? sx : kx), dm * ((f & 2) ? sx : kx), dm * ((f & 4) ? sy : ky),
                                      dm * ((f & 8) ? sy : ky));
-        s_tab[2 * tid + 1] = make_float4(dm * ((f & 16) ? sz : kz), dm * ((f & 32) ? sz : kz),
+        s_tab[3 * tid + 1] = make_float4(dm * ((f & 16) ? sz : kz), dm * ((f & 32) ? sz : kz),
                                          pore ? P.dtt1[f] : 0.f, pore ? P.dtt2[f] : 0.f);
     }
-    // lab-frame phase of this thread's 4 columns (KSPACE), FP64-reduced arguments
+    // lab-frame phases (KSPACE), FP64-reduced arguments, each computed once
+    // per CTA: the tile's 128 columns by threads 0..127, its 8 rows by threads
+    // 128..135, the chunk's planes by the threads from 136 on (wrapping)
+    if constexpr (SCHEME == SCHEME_KSPACE) {
+        if (tid < TW) lab_phase<float>(si->knext[0], x0 + tid, P.dxd, s_ex[tid].x, s_ex[tid].y);
+        else if (tid < TW + TH) lab_phase<float>(si->knext[1], y0 + tid - TW, P.dyd, s_ey[tid - TW].x, s_ey[tid - TW].y);
+        for (int q = (tid + NT - (TW + TH)) % NT; q < z1 - z0; q += NT)
+            lab_phase<float>(si->knext[2], z0 + q, P.dzd, s_ez[q].x, s_ez[q].y);
+    }
+    __syncthreads();
     float exr[QX] = {1.f, 1.f, 1.f, 1.f}, exi[QX] = {0.f, 0.f, 0.f, 0.f};
     if constexpr (SCHEME == SCHEME_KSPACE) {
 #pragma unroll
-        for (int i = 0; i < QX; ++i) lab_phase<float>(si->knext[0], xb + i, P.dxd, exr[i], exi[i]);
-        if (tid < TH) lab_phase<float>(si->knext[1], y0 + tid, P.dyd, s_ey[tid].x, s_ey[tid].y);
-        for (int q = tid; q < z1 - z0; q += NT) lab_phase<float>(si->knext[2], z0 + q, P.dzd, s_ez[q].x, s_ez[q].y);
+        for (int i = 0; i < QX; ++i) {
+            const float2 e = s_ex[QX * lane + i];
+            exr[i] = e.x;
+            exi[i] = e.y;
+        }
     }
-    __syncthreads();
 
     // per-step uniforms
     float gdx = 0.f, gdy = 0.f, gdz = 0.f;
@@ -358,7 +375,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
 #pragma unroll
         for (int i = 0; i < QX; ++i) {
             const uint32_t cd = (code4 >> (8 * i)) & 127u;
-            const float4 ta = s_tab[2 * cd], tb = s_tab[2 * cd + 1];
+            const float4 ta = s_tab[3 * cd], tb = s_tab[3 * cd + 1];
             float wxm = ta.x, wxp = ta.y, wym = ta.z, wyp = ta.w, wzm = tb.x, wzp = tb.y;
             const float dtt1 = tb.z, dtt2 = tb.w;
             if constexpr (VEL) {
