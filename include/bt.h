@@ -49,8 +49,16 @@ extern "C" {
  *   frame of the wave vector k(t) = gamma * int G dt, accumulated in FP64 on
  *   the host, and enters the stencil as per-step face phase factors.
  *   Fields passed in and out are always in the lab frame. */
+/* BT_SCHEME_MACCORMACK: the reference's GPU scheme (solve_gpu's
+ *   ExplicitMakUpgrade, src/NmrRelaxationSolveKernels.cu:637-967,1473-1498):
+ *   predictor with backward-difference advection on the cell-average velocity,
+ *   corrector M' = 0.5 (M + P + rates(P)) with forward differences, face
+ *   diffusivity 2DaDb/(Da+Db+1e-25); a solid neighbour in an advective
+ *   difference holds the voxel's own value (the zero-flux reading of the
+ *   reference's reflection writes). Two launches per step, generic kernel. */
 #define BT_SCHEME_REFERENCE 0
 #define BT_SCHEME_KSPACE 1
+#define BT_SCHEME_MACCORMACK 2
 
 typedef struct bt_config {
     int nx, ny, nz;        /* interior cells (Nmr_start.dat: ik, jk, kk) */
@@ -135,6 +143,30 @@ int bt_run(bt_handle* h, long long nsteps, double* mt_out);
 /* Asynchronous form for timing and pipelines: M(t) stays in the handle's
  * device buffer; bt_read_mt copies the sums of the last bt_run_async. */
 int bt_run_async(bt_handle* h, long long nsteps);
+
+/* Per-voxel relaxation and diffusion, for inputs the uniform-fluid
+ * coefficients cannot express: SurfRel*.dat face relaxivities and two-component
+ * (NCOMP 2) fluids. t1, t2 (s) and diff (m^2/s) are dense [nz][ny][nx] arrays
+ * holding what the reference's FillInDiffusinAndTime leaves in relTime.t1,
+ * relTime.t2 and diffusion (cpp:1756-1841; solid voxels are ignored). The step
+ * then uses dTime*(1/T1), dTime*(1/T2) and the harmonic-mean face diffusivities
+ * 2*Da*Db/(Da+Db+1e-50) of ExplicitSimple (cpp:3174-3185), formed here in FP64 in
+ * that order (domain faces pair a voxel with itself, as the ghost copy does).
+ * All three NULL returns to the coefficients formed from bt_config. Such steps
+ * run on the generic kernel (the FP32 TMA fast path is skipped). */
+int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const double* diff);
+
+/* Two-component M(t) (OutputX/Y/Z with NCOMP 2, cpp:3324-3350, written by
+ * solve_gpu as "Time; X1; Y1; Z1; X2; Y2; Z2", cu:1211-1217): c1, c2 are the
+ * dense [nz][ny][nx] phase fractions (the reference's z1/z2 interpolation of
+ * the concentrations). After every step the library sums c1*M and c2*M over
+ * pore voxels of the trimming box where c1 > 0.8 or c2 > 0.8. Reference scheme,
+ * one field per handle. NULL, NULL switches the sums off. */
+int bt_set_phase_weights(bt_handle* h, const double* c1, const double* c2);
+
+/* The two-component sums of the last run: 6*nsteps doubles, per step
+ * {x1, y1, z1, x2, y2, z2}. */
+int bt_read_mt_phases(bt_handle* h, double* out, long long nsteps);
 
 /* Ragged batch: advance n independent handles (each with its own grid size,
  * geometry and schedule) by nsteps each, asynchronously. Launches are

@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(PKG, "_build", "libbt.so")
 
 BT_OK = 0
 BT_F32, BT_F64 = 0, 1
-BT_SCHEME_REFERENCE, BT_SCHEME_KSPACE = 0, 1
+BT_SCHEME_REFERENCE, BT_SCHEME_KSPACE, BT_SCHEME_MACCORMACK = 0, 1, 2
 GAMMA_REFERENCE = 4.78941714e7   # the reference's hard-coded g (cpp:807)
 GAMMA_PROTON = 2.675e8            # rad/s/T
 
@@ -67,7 +67,8 @@ class Conv3dArgs(ctypes.Structure):
 EXPORTS = [
     "bt_create", "bt_destroy", "bt_last_error", "bt_upload_geometry", "bt_set_state", "bt_get_state",
     "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
-    "bt_run_many", "bt_read_mt", "bt_synchronize", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
+    "bt_run_many", "bt_read_mt", "bt_synchronize", "bt_upload_rates", "bt_set_phase_weights",
+    "bt_read_mt_phases", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
     "bt_version", "bt_autotune", "bt_step_noalloc",
     "bt_conv3d_margin", "bt_conv3d", "bt_conv3d_weight_grad", "bt_conv3d_wgrad_scratch", "bt_conv3d_pack_weights",
     "bt_adamw", "bt_umma_selftest", "bt_field_device",
@@ -100,6 +101,9 @@ def lib():
         "bt_run": ([vp, ll, dp], i),
         "bt_run_async": ([vp, ll], i),
         "bt_run_many": ([ctypes.POINTER(vp), i, ll], i),
+        "bt_upload_rates": ([vp, dp, dp, dp], i),
+        "bt_set_phase_weights": ([vp, dp, dp], i),
+        "bt_read_mt_phases": ([vp, dp, ll], i),
         "bt_read_mt": ([vp, dp, ll], i),
         "bt_synchronize": ([vp], i),
         "bt_stream": ([vp], vp),
@@ -218,6 +222,28 @@ class Solver:
             assert vx.shape == (nz, ny, nx + 1) and vy.shape == (nz, ny + 1, nx) and vz.shape == (nz + 1, ny, nx)
             self._check(self._l.bt_upload_geometry(self._h, mask.ctypes.data, _dp(vx), _dp(vy), _dp(vz)),
                         "upload_geometry")
+
+    def upload_rates(self, t1=None, t2=None, diff=None):
+        """Per-voxel T1, T2 (s) and D (m^2/s), dense (nz, ny, nx); None resets."""
+        if t1 is None and t2 is None and diff is None:
+            self._check(self._l.bt_upload_rates(self._h, None, None, None), "upload_rates")
+            return
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(self.shape) for a in (t1, t2, diff)]
+        self._check(self._l.bt_upload_rates(self._h, *(_dp(a) for a in arrs)), "upload_rates")
+
+    def set_phase_weights(self, c1=None, c2=None):
+        """Two-component sums over c1 / c2 phase fractions, dense (nz, ny, nx); None switches off."""
+        if c1 is None and c2 is None:
+            self._check(self._l.bt_set_phase_weights(self._h, None, None), "set_phase_weights")
+            return
+        a, b = (np.ascontiguousarray(x, dtype=np.float64).reshape(self.shape) for x in (c1, c2))
+        self._check(self._l.bt_set_phase_weights(self._h, _dp(a), _dp(b)), "set_phase_weights")
+
+    def read_mt_phases(self, nsteps):
+        """(nsteps, 6): {x1, y1, z1, x2, y2, z2} after each step of the last run."""
+        out = np.zeros((max(1, nsteps), 6))
+        self._check(self._l.bt_read_mt_phases(self._h, _dp(out), int(nsteps)), "read_mt_phases")
+        return out[:nsteps]
 
     def set_state(self, state):
         """state: (3, nz, ny, nx), or (B, 3, nz, ny, nx) for a batch of B fields."""

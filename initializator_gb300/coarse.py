@@ -56,10 +56,12 @@ def _blocks(t):
     return v.permute(*range(n), n, n + 2, n + 4, n + 1, n + 3, n + 5)  # [..., Z, Y, X, dz, dy, dx]
 
 
-def restrict(f, k, dxf):
+def restrict(f, k, dxf, mask_f=None):
     """Fine field (three tensors [..., nz, ny, nx]: Re, Im in the frame of k,
     and Mz) -> coarse field in the same frame: the mean of the 8 fine cells'
-    lab-frame values, re-expressed at the coarse cell centre."""
+    lab-frame values, re-expressed at the coarse cell centre. With mask_f the
+    mean is over the cell's fine pore voxels instead (the pore average; zero
+    where a coarse cell holds no pore)."""
     import torch
     ph = torch.as_tensor(sub_phases(k, dxf), dtype=f[0].dtype, device=f[0].device)
     cr, ci = ph[..., 0], ph[..., 1]
@@ -67,22 +69,30 @@ def restrict(f, k, dxf):
     re = (cr * mr - ci * mi).mean(dim=(-3, -2, -1))
     im = (cr * mi + ci * mr).mean(dim=(-3, -2, -1))
     mz = _blocks(f[2]).mean(dim=(-3, -2, -1))
-    return [re.contiguous(), im.contiguous(), mz.contiguous()]
+    out = [re, im, mz]
+    if mask_f is not None:
+        mk = torch.as_tensor(np.asarray(mask_f), device=f[0].device).to(f[0].dtype)
+        npore = _blocks(mk).sum(dim=(-3, -2, -1))
+        scale = torch.where(npore > 0, 8.0 / npore.clamp(min=1), torch.zeros_like(npore))
+        out = [t * scale for t in out]
+    return [t.contiguous() for t in out]
 
 
-def prolong(c, k, dxf, mask_f):
-    """Coarse field -> fine field: each coarse value, divided by the pore
-    fraction of its cell, is copied into the cell's fine pore voxels with the
-    restriction's phase undone; fine solid voxels get 0. restrict(prolong(c))
-    == c on every coarse cell that holds pore."""
+def prolong(c, k, dxf, mask_f, pore_average=False):
+    """Coarse field -> fine field: each coarse value (a cell average, divided
+    by the pore fraction of its cell; or, with pore_average, a pore average as
+    it is) is copied into the cell's fine pore voxels with the restriction's
+    phase undone; fine solid voxels get 0. restrict(prolong(c)) == c on every
+    coarse cell that holds pore (with the same pore_average / mask_f choice)."""
     import torch
     ph = torch.as_tensor(sub_phases(k, dxf), dtype=c[0].dtype, device=c[0].device)
     cr, ci = ph[..., 0], -ph[..., 1]
     Z, Y, X = c[0].shape
     mk = torch.as_tensor(np.asarray(mask_f), device=c[0].device).to(c[0].dtype)
-    npore = _blocks(mk).sum(dim=(-3, -2, -1))
-    scale = torch.where(npore > 0, 8.0 / npore.clamp(min=1), torch.zeros_like(npore))
-    c = [t * scale for t in c]
+    if not pore_average:
+        npore = _blocks(mk).sum(dim=(-3, -2, -1))
+        scale = torch.where(npore > 0, 8.0 / npore.clamp(min=1), torch.zeros_like(npore))
+        c = [t * scale for t in c]
 
     def spread(t):
         return t[:, :, :, None, None, None].expand(Z, Y, X, 2, 2, 2)
@@ -122,3 +132,19 @@ def kvec(wave, gamma, dt, n):
     for s in range(n):
         k = k + gamma * w[s] * dt
     return k
+
+
+def lab_sums(field, k, d, weight=None):
+    """Lab-frame sums of a KSPACE field (three tensors [nz][ny][nx]) whose
+    transverse part is in the frame of k: sum of w * exp(-i k.r) m, r the voxel
+    centres ((i + 0.5) d); w = 1 or a per-voxel weight. Returns (x, y, z), FP64."""
+    import torch
+    nz, ny, nx = field[0].shape
+    dev = field[0].device
+    ax = [torch.exp(-1j * torch.as_tensor(k[a] * (np.arange(n) + 0.5) * d[a], device=dev))
+          for a, n in ((0, nx), (1, ny), (2, nz))]
+    ph = ax[2][:, None, None] * ax[1][None, :, None] * ax[0][None, None, :]
+    m = field[0].double() + 1j * field[1].double()
+    w = 1.0 if weight is None else torch.as_tensor(weight, device=dev, dtype=torch.float64)
+    s = (w * ph * m).sum()
+    return np.array([float(s.real), float(s.imag), float((w * field[2].double()).sum())])

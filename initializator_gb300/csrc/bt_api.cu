@@ -71,6 +71,16 @@ struct bt_handle {
     bt::TmaMaps maps[2];
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long launches = 0;
+    // per-voxel mode: [8][nz][ny][pitch] in the handle's precision: dTime/T1,
+    // dTime/T2, then the face diffusivities -x +x -y +y -z +z
+    void* fields_d = nullptr;
+    void* pred_base = nullptr;    // MacCormack predictor field [batch][component][z][y][pitch]
+    // two-component sums: weights [2][nz][ny][pitch], block partials, M(t) x 6
+    void* weights_d = nullptr;
+    double* part6_d = nullptr;
+    double* mt6_d = nullptr;
+    long long mt6_cap = 0;
+    std::vector<uint8_t> mask_h;  // host copy of the pore mask (two-component sums)
 };
 
 namespace {
@@ -155,8 +165,11 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
         }
         P.b = (T)(dTime * c.gamma);
         P.dx = (T)c.dx; P.dy = (T)c.dy; P.dz = (T)c.dz;
-        P.dpp = (T)(2.0 * (D * D) / (D + D + SMALL));
-        P.dps = (T)(2.0 * (SMALL * D) / (SMALL + D + SMALL));
+        // ExplicitSimple regularises the harmonic mean with 1e-50, the GPU
+        // MacCormack kernels with 1e-25
+        const double reg = c.scheme == BT_SCHEME_MACCORMACK ? 1.0e-25 : SMALL;
+        P.dpp = (T)(2.0 * (D * D) / (D + D + reg));
+        P.dps = (T)(2.0 * (SMALL * D) / (SMALL + D + reg));
         // FillInDiffusinAndTime (cpp:1795-1841): bulk rate, then rho/d per solid
         // face in the order -x, +x, -y, +y, -z, +z; tau = 1/(1/rate) as ExplicitSimple reads it
         for (int f = 0; f < 64; ++f) {
@@ -183,6 +196,9 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
         P.partials = h->partials_d;
         P.mt = h->mt_d;
         P.mt_cap = h->mt_cap;
+        P.fstride = (long long)h->comp;
+        P.fdtt = h->fields_d ? static_cast<const T*>(h->fields_d) : nullptr;
+        P.fw = h->fields_d ? static_cast<const T*>(h->fields_d) + 2 * h->comp : nullptr;
     }
 }
 
@@ -297,13 +313,37 @@ bool step_has_pulse(const bt_handle* h, long long s) {
 
 cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
     const bt_config& c = h->cfg;
-    const int prec = (c.scheme == BT_SCHEME_REFERENCE && c.vector_mult == 1) ? 1 : 0;
+    const int prec = (c.scheme != BT_SCHEME_KSPACE && c.vector_mult == 1) ? 1 : 0;
     const int vel = c.velocity == 1 ? 1 : 0;
     h->launches++;
-    if (c.precision == BT_F64) return bt::launch_step<double>(h->pd[side], c.scheme, vel, prec, h->grid, h->stream);
-    if (h->use_tma && !step_has_pulse(h, abs_step))
-        return bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, h->stream);
-    return bt::launch_step<float>(h->pf[side], c.scheme, vel, prec, h->grid, h->stream);
+    cudaError_t e;
+    if (c.scheme == BT_SCHEME_MACCORMACK) {
+        h->launches++;  // predictor + corrector
+        char* pb = static_cast<char*>(h->pred_base);
+        if (c.precision == BT_F64) {
+            double* pr[3] = {(double*)pb, (double*)(pb + 8 * h->comp), (double*)(pb + 16 * h->comp)};
+            e = bt::launch_mac<double>(h->pd[side], pr, vel, prec, h->grid, h->stream);
+        } else {
+            float* pr[3] = {(float*)pb, (float*)(pb + 4 * h->comp), (float*)(pb + 8 * h->comp)};
+            e = bt::launch_mac<float>(h->pf[side], pr, vel, prec, h->grid, h->stream);
+        }
+    } else if (c.precision == BT_F64)
+        e = bt::launch_step<double>(h->pd[side], c.scheme, vel, prec, h->grid, h->stream);
+    else if (h->use_tma && !h->fields_d && !step_has_pulse(h, abs_step))
+        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, h->stream);
+    else
+        e = bt::launch_step<float>(h->pf[side], c.scheme, vel, prec, h->grid, h->stream);
+    if (e != cudaSuccess || !h->weights_d) return e;
+    // two-component sums of the field this step wrote
+    h->launches += 2;
+    if (c.precision == BT_F64) {
+        const double* w = static_cast<const double*>(h->weights_d);
+        return bt::launch_phase_sums<double>(h->pd[side], w, w + h->comp, h->part6_d, SUMS_BLOCKS, h->mt6_d,
+                                             h->mt6_cap, h->stream);
+    }
+    const float* w = static_cast<const float*>(h->weights_d);
+    return bt::launch_phase_sums<float>(h->pf[side], w, w + h->comp, h->part6_d, SUMS_BLOCKS, h->mt6_d, h->mt6_cap,
+                                        h->stream);
 }
 
 // per-step table: gradient, KSPACE wave vector and face phases, pulse ranges
@@ -391,6 +431,15 @@ void kvec_at(const bt_handle* h, long long s, int b, double k[3]) {
 }
 
 int ensure_mt(bt_handle* h, long long n) {
+    if (h->weights_d && n > h->mt6_cap) {
+        const long long cap = std::max<long long>(n, 1024);
+        if (h->mt6_d) cudaFree(h->mt6_d);
+        h->mt6_d = nullptr;
+        h->mt6_cap = 0;
+        drop_graphs(h);  // captured launches hold the old buffer
+        CK(h, cudaMalloc(&h->mt6_d, sizeof(double) * 6 * cap));
+        h->mt6_cap = cap;
+    }
     if (n <= h->mt_cap) return BT_OK;
     long long cap = std::max<long long>(n, 1024);
     if (h->mt_d) cudaFree(h->mt_d);
@@ -488,7 +537,8 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     *out = nullptr;
     if (cfg->nx <= 0 || cfg->ny <= 0 || cfg->nz <= 0) return BT_E_ARG;
     if (cfg->precision != BT_F32 && cfg->precision != BT_F64) return BT_E_ARG;
-    if (cfg->scheme != BT_SCHEME_REFERENCE && cfg->scheme != BT_SCHEME_KSPACE) return BT_E_ARG;
+    if (cfg->scheme != BT_SCHEME_REFERENCE && cfg->scheme != BT_SCHEME_KSPACE && cfg->scheme != BT_SCHEME_MACCORMACK)
+        return BT_E_ARG;
     if (!(cfg->dt > 0) || !(cfg->dx > 0) || !(cfg->dy > 0) || !(cfg->dz > 0)) return BT_E_ARG;
     for (int a = 0; a < 3; ++a)
         if (cfg->buffer[a] < 0 || 2 * cfg->buffer[a] > (a == 0 ? cfg->nx : a == 1 ? cfg->ny : cfg->nz)) return BT_E_ARG;
@@ -527,6 +577,11 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
         cudaMemset(h->state_base[s], 0, sbytes);
         for (int k = 0; k < 3; ++k) h->state[s][k] = static_cast<char*>(h->state_base[s]) + k * h->esz * h->comp;
     }
+    if (cfg->scheme == BT_SCHEME_MACCORMACK) {
+        // the predictor's field (zero in solid, as the reference's memset)
+        if (cudaMalloc(&h->pred_base, sbytes) != cudaSuccess) return bail(BT_E_NOMEM);
+        cudaMemset(h->pred_base, 0, sbytes);
+    }
     const size_t cbytes = (size_t)h->cpitch * cfg->ny * cfg->nz;
     if (cudaMalloc(&h->code, cbytes) != cudaSuccess) return bail(BT_E_NOMEM);
     cudaMemset(h->code, 0, cbytes);
@@ -552,7 +607,7 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     if (rc) return bail(rc);
     rc = build_schedule(h, nullptr, 0, nullptr, 0);
     if (rc) return bail(rc);
-    if (cfg->precision == BT_F32 && !std::getenv("BT_NO_TMA")) {
+    if (cfg->precision == BT_F32 && cfg->scheme != BT_SCHEME_MACCORMACK && !std::getenv("BT_NO_TMA")) {
         rc = set_tma_split(h, default_tma_split(h));
         if (rc) return bail(rc);
     }
@@ -576,6 +631,11 @@ int bt_destroy(bt_handle* h) {
     if (h->staging) cudaFreeHost(h->staging);
     if (h->partials_d) cudaFree(h->partials_d);
     if (h->mt_d) cudaFree(h->mt_d);
+    if (h->fields_d) cudaFree(h->fields_d);
+    if (h->pred_base) cudaFree(h->pred_base);
+    if (h->weights_d) cudaFree(h->weights_d);
+    if (h->part6_d) cudaFree(h->part6_d);
+    if (h->mt6_d) cudaFree(h->mt6_d);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return BT_OK;
@@ -587,6 +647,7 @@ int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, cons
     if (!h || !mask) return fail(h, BT_E_ARG, "mask is required");
     const bt_config& c = h->cfg;
     if (c.velocity == 1 && (!vx || !vy || !vz)) return fail(h, BT_E_ARG, "velocity == 1 needs vx, vy and vz");
+    h->mask_h.assign(mask, mask + h->nvox);
     uint8_t* mtmp = nullptr;
     CK(h, cudaMalloc(&mtmp, h->nvox));
     cudaError_t e = cudaMemcpy(mtmp, mask, h->nvox, cudaMemcpyHostToDevice);
@@ -616,7 +677,9 @@ int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, cons
         }
     }
     h->geometry = true;
-    if (h->cfg.precision == BT_F32 && h->tgrid.y > 0 && !std::getenv("BT_NO_TMA")) h->use_tma = build_maps(h);
+    if (h->cfg.precision == BT_F32 && h->cfg.scheme != BT_SCHEME_MACCORMACK && h->tgrid.y > 0 &&
+        !std::getenv("BT_NO_TMA"))
+        h->use_tma = build_maps(h);
     refresh_params(h);
     return BT_OK;
 }
@@ -841,6 +904,118 @@ int bt_measure(bt_handle* h, double* sums3) {
 }
 
 long long bt_launch_count(const bt_handle* h) { return h ? h->launches : -1; }
+
+namespace {
+
+// dense [nz][ny][nx] doubles -> count pitched arrays of the handle's precision
+int put_pitched(bt_handle* h, void* dst, const std::vector<double>& src, int count) {
+    const bt_config& c = h->cfg;
+    CK(h, cudaStreamSynchronize(h->stream));
+    const size_t n = (size_t)count * h->comp;
+    if (h->esz == 8) {
+        CK(h, cudaMemcpy(dst, src.data(), n * 8, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> f(n);
+        for (size_t q = 0; q < n; ++q) f[q] = (float)src[q];
+        CK(h, cudaMemcpy(dst, f.data(), n * 4, cudaMemcpyHostToDevice));
+    }
+    (void)c;
+    return BT_OK;
+}
+
+}  // namespace
+
+int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const double* diff) {
+    if (!h) return BT_E_ARG;
+    if (!t1 && !t2 && !diff) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (h->fields_d) cudaFree(h->fields_d);
+        h->fields_d = nullptr;
+        refresh_params(h);
+        return BT_OK;
+    }
+    if (!t1 || !t2 || !diff) return fail(h, BT_E_ARG, "t1, t2 and diff are uploaded together");
+    const bt_config& c = h->cfg;
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    const size_t comp = h->comp;
+    std::vector<double> buf(8 * comp, 0.0);
+    const double dTime = c.dt;
+    const double reg = c.scheme == BT_SCHEME_MACCORMACK ? 1.0e-25 : SMALL;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t q = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
+                const size_t v = ((size_t)k * ny + j) * h->pitch + i;
+                // ExplicitSimple (cpp:3174-3185): tau = 1/relTime, relaxation dTime*tau
+                buf[v] = dTime * (1.0 / t1[q]);
+                buf[comp + v] = dTime * (1.0 / t2[q]);
+                // harmonic-mean face diffusivities; ghosts copy the edge value
+                // (BoundaryConditionsForDiffusion), so a domain face pairs the voxel with itself
+                const double Dc = diff[q];
+                const double nb[6] = {i > 0 ? diff[q - 1] : Dc, i < nx - 1 ? diff[q + 1] : Dc,
+                                      j > 0 ? diff[q - nx] : Dc, j < ny - 1 ? diff[q + nx] : Dc,
+                                      k > 0 ? diff[q - (size_t)nx * ny] : Dc,
+                                      k < nz - 1 ? diff[q + (size_t)nx * ny] : Dc};
+                for (int f = 0; f < 6; ++f) buf[(2 + f) * comp + v] = 2.0 * (nb[f] * Dc) / (nb[f] + Dc + reg);
+            }
+    if (!h->fields_d) {
+        drop_graphs(h);
+        CK(h, cudaMalloc(&h->fields_d, 8 * comp * h->esz));
+    }
+    int rc = put_pitched(h, h->fields_d, buf, 8);
+    if (rc) return rc;
+    refresh_params(h);
+    return BT_OK;
+}
+
+int bt_set_phase_weights(bt_handle* h, const double* c1, const double* c2) {
+    if (!h) return BT_E_ARG;
+    if (!c1 && !c2) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        drop_graphs(h);
+        if (h->weights_d) cudaFree(h->weights_d);
+        if (h->part6_d) cudaFree(h->part6_d);
+        h->weights_d = nullptr;
+        h->part6_d = nullptr;
+        return BT_OK;
+    }
+    if (!c1 || !c2) return fail(h, BT_E_ARG, "c1 and c2 are set together");
+    if (h->nb > 1) return fail(h, BT_E_ARG, "two-component sums take one field per handle");
+    if (h->cfg.scheme == BT_SCHEME_KSPACE) return fail(h, BT_E_ARG, "two-component sums are lab-frame sums: not KSPACE");
+    if (!h->geometry || !h->mask_h.size()) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    const bt_config& c = h->cfg;
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    const size_t comp = h->comp;
+    std::vector<double> buf(2 * comp, 0.0);
+    const int x0 = c.buffer[0], x1 = nx - c.buffer[0], y0 = c.buffer[1], y1 = ny - c.buffer[1];
+    const int z0 = c.buffer[2], z1 = nz - c.buffer[2];
+    for (int k = z0; k < z1; ++k)
+        for (int j = y0; j < y1; ++j)
+            for (int i = x0; i < x1; ++i) {
+                const size_t q = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
+                // OutputX/Y/Z (cpp:3324-3350): pore voxels where one phase exceeds 0.8
+                if (!h->mask_h[q] || !(c1[q] > 0.8 || c2[q] > 0.8)) continue;
+                const size_t v = ((size_t)k * ny + j) * h->pitch + i;
+                buf[v] = c1[q];
+                buf[comp + v] = c2[q];
+            }
+    if (!h->weights_d) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        drop_graphs(h);
+        CK(h, cudaMalloc(&h->weights_d, 2 * comp * h->esz));
+        CK(h, cudaMalloc(&h->part6_d, sizeof(double) * 6 * SUMS_BLOCKS));
+    }
+    return put_pitched(h, h->weights_d, buf, 2);
+}
+
+int bt_read_mt_phases(bt_handle* h, double* out, long long nsteps) {
+    if (!h || !out || nsteps < 0 || nsteps > h->last_run) return fail(h, BT_E_ARG, "bad two-component M(t) read");
+    if (!h->weights_d) return fail(h, BT_E_STATE, "bt_set_phase_weights first");
+    int rc = check_ctl(h);
+    if (rc) return rc;
+    if (nsteps > 0) CK(h, cudaMemcpy(out, h->mt6_d, sizeof(double) * 6 * nsteps, cudaMemcpyDeviceToHost));
+    return BT_OK;
+}
 
 int bt_field_device(bt_handle* h, int member, void** mx, void** my, void** mz, int* pitch) {
     if (!h || member < 0 || member >= h->nb || !mx || !my || !mz || !pitch) return fail(h, BT_E_ARG, "bad field query");

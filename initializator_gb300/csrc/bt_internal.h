@@ -83,6 +83,14 @@ struct StepParams {
     double* partials;           // [nbatch][CTAs per member][3]
     double* mt;                 // [mt_cap][nbatch][3]
     long long mt_cap;           // steps
+    // per-voxel mode (SurfRel*.dat face relaxivities, two-component fluids):
+    // when fdtt is set the kernel reads dTime/T1, dTime/T2 from fdtt[0 / fstride
+    // + v] and the six face diffusivities (-x +x -y +y -z +z) from
+    // fw[f * fstride + v] instead of the code tables; v = z * plane + y * pitch + x
+    const T* fdtt;
+    const T* fw;
+    long long fstride;
+    const T* orig[3];           // MacCormack corrector: the step's input field M
 };
 
 // TMA descriptors of the FP32 fast path (one per ping-pong input side)
@@ -96,6 +104,13 @@ template <typename T>
 cudaError_t launch_step(const StepParams<T>& p, int scheme, int vel, int prec, dim3 grid, cudaStream_t s);
 template <typename T>
 cudaError_t launch_sums(const StepParams<T>& p, double* out4, cudaStream_t s);
+// MacCormack step (predictor into pred, then corrector into p.out)
+template <typename T>
+cudaError_t launch_mac(const StepParams<T>& p, T* const pred[3], int vel, int prec, dim3 grid, cudaStream_t s);
+// two-component weighted sums of the newest field into mt6 (6 per step)
+template <typename T>
+cudaError_t launch_phase_sums(const StepParams<T>& p, const T* w1, const T* w2, double* part6, int nblocks,
+                              double* mt6, long long cap, cudaStream_t s);
 // FP32 fast path: TMA-staged plane tiles, 4 voxels per thread, no pulses
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
                             cudaStream_t s);

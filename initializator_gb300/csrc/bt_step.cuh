@@ -320,7 +320,9 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
             T o0 = 0, o1 = 0, o2 = 0;
             if (cd & CODE_PORE) {
                 const int f = cd & 63;
-                const T dtt1 = P.dtt1[f], dtt2 = P.dtt2[f];
+                const long long vox = oz + col;
+                const T dtt1 = P.fdtt ? P.fdtt[vox] : P.dtt1[f];
+                const T dtt2 = P.fdtt ? P.fdtt[P.fstride + vox] : P.dtt2[f];
                 const T px0 = cc[0], py0 = cc[1], pz0 = cc[2];
                 // neighbours: -x +x -y +y -z +z, per component
                 T nb[3][6];
@@ -385,9 +387,17 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
                     az = a[2];
                 }
                 if (P.diffusion) {
-                    const T dxm = (f & 1) ? P.dps : P.dpp, dxp = (f & 2) ? P.dps : P.dpp;
-                    const T dym = (f & 4) ? P.dps : P.dpp, dyp = (f & 8) ? P.dps : P.dpp;
-                    const T dzm = (f & 16) ? P.dps : P.dpp, dzp = (f & 32) ? P.dps : P.dpp;
+                    T dxm = (f & 1) ? P.dps : P.dpp, dxp = (f & 2) ? P.dps : P.dpp;
+                    T dym = (f & 4) ? P.dps : P.dpp, dyp = (f & 8) ? P.dps : P.dpp;
+                    T dzm = (f & 16) ? P.dps : P.dpp, dzp = (f & 32) ? P.dps : P.dpp;
+                    if (P.fw) {
+                        dxm = P.fw[vox];
+                        dxp = P.fw[P.fstride + vox];
+                        dym = P.fw[2 * P.fstride + vox];
+                        dyp = P.fw[3 * P.fstride + vox];
+                        dzm = P.fw[4 * P.fstride + vox];
+                        dzp = P.fw[5 * P.fstride + vox];
+                    }
                     const T p0[3] = {px0, py0, pz0};
                     T a[3] = {ax, ay, az};
 #pragma unroll
@@ -497,6 +507,80 @@ __global__ void sums_kernel(const __grid_constant__ StepParams<T> P, double kx, 
             for (int c = 0; c < 4; ++c) t[c] += red[w][c];
 #pragma unroll
         for (int c = 0; c < 4; ++c) P.partials[4ull * blockIdx.x + c] = t[c];
+    }
+}
+
+// two-component sums (OutputX/Y/Z with NCOMP 2, cpp:3324-3350): per block,
+// sum of w1 * M and w2 * M over the newest field (P.out), FP64, in a fixed
+// order; w1 / w2 are zero where a voxel is not counted. part6[block][6] =
+// {x1, y1, z1, x2, y2, z2}
+template <typename T>
+__global__ void phase_sums_kernel(const __grid_constant__ StepParams<T> P, const T* w1, const T* w2, double* part6) {
+    __shared__ double red[NTHREADS / 32][6];
+    const int tid = threadIdx.x;
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const long long n = (long long)P.nx * P.ny * P.nz;
+    for (long long qq = blockIdx.x * (long long)NTHREADS + tid; qq < n; qq += (long long)gridDim.x * NTHREADS) {
+        const int x = (int)(qq % P.nx), y = (int)((qq / P.nx) % P.ny), z = (int)(qq / ((long long)P.nx * P.ny));
+        const long long q = ((long long)z * P.ny + y) * P.pitch + x;
+        const double a = (double)w1[q], b = (double)w2[q];
+        if (a == 0.0 && b == 0.0) continue;
+        const double mx = (double)P.out[0][q], my = (double)P.out[1][q], mz = (double)P.out[2][q];
+        s[0] += mx * a;
+        s[1] += my * a;
+        s[2] += mz * a;
+        s[3] += mx * b;
+        s[4] += my * b;
+        s[5] += mz * b;
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+    if ((tid & 31) == 0)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) red[tid >> 5][c] = s[c];
+    __syncthreads();
+    if (tid == 0) {
+        double t[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int w = 0; w < NTHREADS / 32; ++w)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) t[c] += red[w][c];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) part6[6ull * blockIdx.x + c] = t[c];
+    }
+}
+
+// one block: the blocks' partials in a fixed order -> mt6[slot], slot = the
+// step just taken (the step kernel has advanced the device counter)
+static __global__ void phase_finish_kernel(const Ctl* ctl, const double* part6, int nblocks, double* mt6, long long cap,
+                                    int* status) {
+    __shared__ double red[NTHREADS / 32][6];
+    const int tid = threadIdx.x;
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int q = tid; q < nblocks; q += NTHREADS)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s[c] += part6[6 * q + c];
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+    if ((tid & 31) == 0)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) red[tid >> 5][c] = s[c];
+    __syncthreads();
+    if (tid == 0) {
+        double t[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int w = 0; w < NTHREADS / 32; ++w)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) t[c] += red[w][c];
+        const long long slot = __ldcg(&ctl->step) - 1 - __ldcg(&ctl->mt_base);
+        if (slot >= 0 && slot < cap) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) mt6[6 * slot + c] = t[c];
+        } else {
+            atomicOr(status, 1);
+        }
     }
 }
 

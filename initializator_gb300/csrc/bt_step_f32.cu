@@ -1,6 +1,7 @@
 // float instantiation of the fused step kernel and its helpers.
 // Compiled with the default -fmad=true (FP32 production path).
 #include "bt_step_tma.cuh"
+#include "bt_step_mac.cuh"
 
 namespace bt {
 
@@ -14,6 +15,19 @@ cudaError_t launch_sums<float>(const StepParams<float>& p, double* kvec_and_grid
     // kvec_and_grid: {kx, ky, kz, nblocks}
     const int nblocks = (int)kvec_and_grid[3];
     sums_kernel<float><<<nblocks, NTHREADS, 0, s>>>(p, kvec_and_grid[0], kvec_and_grid[1], kvec_and_grid[2], p.partials);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t launch_mac<float>(const StepParams<float>& p, float* const pred[3], int vel, int prec, dim3 grid, cudaStream_t s) {
+    return launch_mac_impl<float>(p, pred, vel, prec, grid, s);
+}
+
+template <>
+cudaError_t launch_phase_sums<float>(const StepParams<float>& p, const float* w1, const float* w2, double* part6, int nblocks,
+                                double* mt6, long long cap, cudaStream_t s) {
+    phase_sums_kernel<float><<<nblocks, NTHREADS, 0, s>>>(p, w1, w2, part6);
+    phase_finish_kernel<<<1, NTHREADS, 0, s>>>(p.ctl, part6, nblocks, mt6, cap, &p.ctl->status);
     return cudaGetLastError();
 }
 

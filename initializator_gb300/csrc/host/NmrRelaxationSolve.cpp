@@ -62,8 +62,7 @@ void NmrRelaxationSolve::init() {
     const nmr::Data& d = data_;
     std::cout << "X grid size" << nx_ << std::endl << "Y grid size" << ny_ << std::endl
               << "Z grid size" << nz_ << std::endl;
-    if (d.nComponents != 1) die("NCOMP = 2 (two-phase mixing) is not supported by this solver");
-    if (d.nSurfRelWater == 1 || d.nSurfRelOil == 1) die("SurfRel*.dat face relaxivities are not supported");
+    if (d.nComponents != 1 && d.nComponents != 2) die("NCOMP must be 1 or 2");
     if (d.noiseAmpl != 0.0 && d.nDirectionField != 0)
         die("AMPL_NOISE != 0 (an unseeded random noise field) is not supported");
 
@@ -99,30 +98,90 @@ void NmrRelaxationSolve::init() {
         dTimeVel_ = cfl_edge_limit(d.dx, d.dy, d.dz, d.cfl, vm + kSmall, false);
     }
 
-    // rates and the diffusion / relaxation limits (FillInDiffusinAndTime, cpp:1756-1863)
-    const bool water = d.nFluid == 1;
-    const double c1 = water ? 1.0 : 0.0, c2 = water ? 0.0 : 1.0;
-    const double D = c1 * d.dWater + c2 * d.dOil;
+    // phase fractions: FillInConcentration (cpp:935-1008), then for two
+    // components the z1/z2 interpolation between the phase points (cpp:1780-1786)
+    const size_t nvox = (size_t)nx_ * ny_ * nz_;
+    c1_.assign(nvox, 0.0);
+    c2_.assign(nvox, 0.0);
+    if (d.nComponents == 2) {
+        std::vector<double> n1;
+        if (!nmr::read_n1("data/n1_init.dat", nx_, ny_, nz_, n1, err)) die("Caught exception: " + err);
+        for (size_t q = 0; q < nvox; ++q) {
+            const double a = n1[q], b = 1.0 - n1[q];
+            const double z1 = std::sqrt((a - d.an1) * (a - d.an1) + (b - d.an2) * (b - d.an2));
+            const double z2 = std::sqrt((a - d.bn1) * (a - d.bn1) + (b - d.bn2) * (b - d.bn2));
+            c1_[q] = z2 / (z1 + z2);
+            c2_[q] = z1 / (z1 + z2);
+        }
+    } else {
+        for (size_t q = 0; q < nvox; ++q) {
+            c1_[q] = d.nFluid == 1 ? 1.0 : 0.0;
+            c2_[q] = d.nFluid == 2 ? 1.0 : 0.0;
+        }
+    }
+    fields_ = d.nComponents == 2 || d.nSurfRelWater == 1 || d.nSurfRelOil == 1;
+
+    // face relaxivities (ReadSurfRel, cpp:1012-1435): [1Water, 2Water, 1Oil, 2Oil][axis]
+    std::vector<double> sr[4][3];
+    {
+        const char* keys[4] = {"1Water", "2Water", "1Oil", "2Oil"};
+        const int flags[4] = {d.nSurfRelWater, d.nSurfRelWater, d.nSurfRelOil, d.nSurfRelOil};
+        const double consts[4] = {d.r1Water, d.r2Water, d.r1Oil, d.r2Oil};
+        const size_t nface[3] = {(size_t)(nx_ + 1) * ny_ * nz_, (size_t)nx_ * (ny_ + 1) * nz_,
+                                 (size_t)nx_ * ny_ * (nz_ + 1)};
+        for (int s = 0; s < 4; ++s) {
+            if (flags[s] == 1) {
+                if (!nmr::read_surfrel("data", keys[s], nx_, ny_, nz_, sr[s][0], sr[s][1], sr[s][2], err))
+                    die("Caught exception: " + err);
+            } else {
+                for (int a = 0; a < 3; ++a) sr[s][a].assign(nface[a], consts[s]);
+            }
+        }
+    }
+
+    // rates, diffusivity and their limits (FillInDiffusinAndTime, cpp:1756-1863)
     double dMax = 0.0, tMin = 100.0;
     const long long plane = (long long)nx_ * ny_;
     const double dd[3] = {d.dx, d.dy, d.dz};
+    if (fields_) {
+        t1_.assign(nvox, 1.0e50);
+        t2_.assign(nvox, 1.0e50);
+        diff_.assign(nvox, kSmall);
+    }
     for (int k = 0; k < nz_; ++k)
         for (int j = 0; j < ny_; ++j)
             for (int i = 0; i < nx_; ++i) {
                 const long long q = i + (long long)nx_ * j + plane * k;
                 if (!mask_[q]) continue;
+                const double c1 = c1_[q], c2 = c2_[q];
+                const double cd = (c1 * d.dWater + c2 * d.dOil);
+                double Dv = cd * std::pow((1.0 - 2.0 * c1 * c2 / (c1 * c1 + c2 * c2)), 10.0);
+                if (d.nDiffusion == 0) Dv = kSmall;
                 double ct1 = c1 / d.t1Water + c2 / d.t1Oil;
                 double ct2 = c1 / d.t2Water + c2 / d.t2Oil;
                 // out-of-domain neighbours copy the voxel itself: never solid
                 const bool solid[6] = {i > 0 && !mask_[q - 1], i < nx_ - 1 && !mask_[q + 1],
                                        j > 0 && !mask_[q - nx_], j < ny_ - 1 && !mask_[q + nx_],
                                        k > 0 && !mask_[q - plane], k < nz_ - 1 && !mask_[q + plane]};
+                // the face of each neighbour in its axis' face array
+                const size_t fidx[6] = {(size_t)i + (size_t)(nx_ + 1) * ((size_t)j + (size_t)ny_ * k),
+                                        (size_t)(i + 1) + (size_t)(nx_ + 1) * ((size_t)j + (size_t)ny_ * k),
+                                        (size_t)i + (size_t)nx_ * ((size_t)j + (size_t)(ny_ + 1) * k),
+                                        (size_t)i + (size_t)nx_ * ((size_t)(j + 1) + (size_t)(ny_ + 1) * k),
+                                        (size_t)i + (size_t)nx_ * ((size_t)j + (size_t)ny_ * k),
+                                        (size_t)i + (size_t)nx_ * ((size_t)j + (size_t)ny_ * (k + 1))};
                 for (int f = 0; f < 6; ++f)
                     if (solid[f]) {
-                        ct1 += (c1 * d.r1Water + c2 * d.r1Oil) / dd[f / 2];
-                        ct2 += (c1 * d.r2Water + c2 * d.r2Oil) / dd[f / 2];
+                        const int a = f / 2;
+                        const size_t fi = fidx[f];
+                        ct1 += (c1 * sr[0][a][fi] + c2 * sr[2][a][fi]) / dd[a];
+                        ct2 += (c1 * sr[1][a][fi] + c2 * sr[3][a][fi]) / dd[a];
                     }
-                const double Dv = d.nDiffusion == 0 ? kSmall : D;
+                if (fields_) {
+                    t1_[q] = 1.0 / ct1;
+                    t2_[q] = 1.0 / ct2;
+                    diff_[q] = Dv;
+                }
                 if (dMax <= Dv) dMax = Dv;
                 if (tMin >= 1.0 / ct1) tMin = 1.0 / ct1;
                 if (tMin >= 1.0 / ct2) tMin = 1.0 / ct2;
@@ -234,6 +293,9 @@ void NmrRelaxationSolve::run(bool gpu_path) {
     check(bt_upload_geometry(h_, mask_.data(), vx_.empty() ? nullptr : vx_.data(), vy_.empty() ? nullptr : vy_.data(),
                              vz_.empty() ? nullptr : vz_.data()),
           "bt_upload_geometry");
+    const bool two = d.nComponents == 2;
+    if (fields_) check(bt_upload_rates(h_, t1_.data(), t2_.data(), diff_.data()), "bt_upload_rates");
+    if (two) check(bt_set_phase_weights(h_, c1_.data(), c2_.data()), "bt_set_phase_weights");
     std::vector<double> mx, my, mz;
     initial_field(mx, my, mz);
     check(bt_set_state(h_, mx.data(), my.data(), mz.data()), "bt_set_state");
@@ -254,19 +316,49 @@ void NmrRelaxationSolve::run(bool gpu_path) {
     check(bt_sequence_schedule(&sp, iters, pulses.data(), npulses, &npulses), "bt_sequence_schedule");
     check(bt_set_schedule(h_, pulses.data(), npulses, nullptr, 0), "bt_set_schedule");
 
-    double m0[3];
-    check(bt_measure(h_, m0), "bt_measure");
-    std::vector<double> mt(3 * iters);
+    // the sums of one output row: 3 (SumX, SumY, SumZ) or, with two
+    // components, 6 (X1 Y1 Z1 X2 Y2 Z2; OutputX/Y/Z cpp:3324-3350)
+    const int w = two ? 6 : 3;
+    std::vector<double> m0(w, 0.0);
+    if (two) {
+        // the initial field's two-component sums, in the reference's order
+        for (int k = d.bufferZ; k < nz_ - d.bufferZ; ++k)
+            for (int j = d.bufferY; j < ny_ - d.bufferY; ++j)
+                for (int i = d.bufferX; i < nx_ - d.bufferX; ++i) {
+                    const size_t q = (size_t)i + (size_t)nx_ * ((size_t)j + (size_t)ny_ * k);
+                    if (!mask_[q] || !(c1_[q] > 0.8 || c2_[q] > 0.8)) continue;
+                    m0[0] += mx[q] * c1_[q];
+                    m0[3] += mx[q] * c2_[q];
+                    m0[1] += my[q] * c1_[q];
+                    m0[4] += my[q] * c2_[q];
+                    m0[2] += mz[q] * c1_[q];
+                    m0[5] += mz[q] * c2_[q];
+                }
+    } else {
+        check(bt_measure(h_, m0.data()), "bt_measure");
+    }
+    std::vector<double> mt((size_t)w * iters);
+    std::vector<double> mt3(two ? 3 * std::min<long long>(iters, 65536) : 0);
     const long long chunk = 65536;
     for (long long s = 0; s < iters; s += chunk) {
         const long long n = std::min(chunk, iters - s);
-        check(bt_run(h_, n, &mt[3 * s]), "bt_run");
+        if (two) {
+            check(bt_run(h_, n, mt3.data()), "bt_run");
+            check(bt_read_mt_phases(h_, &mt[6 * s], n), "bt_read_mt_phases");
+        } else {
+            check(bt_run(h_, n, &mt[3 * s]), "bt_run");
+        }
     }
     // sums printed at step i: after the step on the GPU path (cu:1187-1219),
     // before it on the CPU path (cpp:38-55)
     auto sums_at = [&](long long i) -> const double* {
-        if (gpu_path) return &mt[3 * i];
-        return i == 0 ? m0 : &mt[3 * (i - 1)];
+        if (gpu_path) return &mt[(size_t)w * i];
+        return i == 0 ? m0.data() : &mt[(size_t)w * (i - 1)];
+    };
+    auto row = [&](std::ostream& o, double t, const double* r) {
+        o << std::scientific << t;
+        for (int c = 0; c < w; ++c) o << "; " << std::scientific << r[c];
+        o << std::endl;
     };
     std::ofstream res(gpu_path ? "results_gpu.csv" : "results_cpu.csv");
     res << "Time; SumX; SumY; SumZ" << std::endl;
@@ -274,9 +366,12 @@ void NmrRelaxationSolve::run(bool gpu_path) {
         if (i % d.ndPrint != 0) continue;
         const double t = i * dTime_;
         const double* r = sums_at(i);
-        std::cout << " Time = " << t << " SumX=" << r[0] << " SumY=" << r[1] << " SumZ=" << r[2] << std::endl;
-        res << std::scientific << t << "; " << std::scientific << r[0] << "; " << std::scientific << r[1] << "; "
-            << std::scientific << r[2] << std::endl;
+        if (two)
+            std::cout << " Time = " << t << " SumX1=" << r[0] << " SumY1=" << r[1] << " SumZ1=" << r[2]
+                      << "\t SumX2=" << r[3] << " SumY2=" << r[4] << " SumZ2=" << r[5] << std::endl;
+        else
+            std::cout << " Time = " << t << " SumX=" << r[0] << " SumY=" << r[1] << " SumZ=" << r[2] << std::endl;
+        row(res, t, r);
     }
     res.close();
     if (gpu_path) {
@@ -286,10 +381,9 @@ void NmrRelaxationSolve::run(bool gpu_path) {
         std::snprintf(name, sizeof(name), "results_NMR/results_grad_%d_%d_%d.csv", PulseNum[0], PulseNum[1],
                       PulseNum[2]);
         std::ofstream rg(name);
-        const double* r = &mt[3 * (iters - 1)];
+        const double* r = &mt[(size_t)w * (iters - 1)];
         std::cout << " SumX=" << r[0] << " SumY=" << r[1] << " SumZ=" << r[2] << std::endl;
-        rg << std::scientific << (iters - 1) * dTime_ << "; " << std::scientific << r[0] << "; " << std::scientific
-           << r[1] << "; " << std::scientific << r[2] << std::endl;
+        row(rg, (iters - 1) * dTime_, r);
     }
     bt_destroy(h_);
     h_ = nullptr;

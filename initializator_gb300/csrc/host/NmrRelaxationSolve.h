@@ -52,6 +52,10 @@ private:
     double pEq_ = 0.0, endTime_ = 0.0, dTime_ = 0.0;
     double dTimeVel_ = 1.0, dTimeDiff_ = 1.0, dTimeRel_ = 1.0, dTimeNoise_ = 0.0, dTimeGrad_ = 0.0;
     int nStep_ = 0;
+    // per-voxel coefficients (SurfRel*.dat or NCOMP 2): T1, T2, D as
+    // FillInDiffusinAndTime forms them, and the phase fractions c1, c2
+    bool fields_ = false;
+    std::vector<double> t1_, t2_, diff_, c1_, c2_;
     bool initialised_ = false;
     bt_handle* h_ = nullptr;
 

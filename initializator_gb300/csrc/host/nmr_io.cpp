@@ -209,4 +209,36 @@ bool read_velocity(const std::string& dir, int nx, int ny, int nz, double vel_mu
     return true;
 }
 
+bool read_surfrel(const std::string& dir, const std::string& key, int nx, int ny, int nz, std::vector<double>& fx,
+                  std::vector<double>& fy, std::vector<double>& fz, std::string& err) {
+    double hi = 0.0, lo = 0.0;
+    const std::string p = dir + "/SurfRel" + key;
+    if (!read_faces(p + "X.dat", nx + 1, ny, nz, 1.0, fx, nx + 1, ny, hi, lo, err)) return false;
+    if (!read_faces(p + "Y.dat", nx, ny + 1, nz, 1.0, fy, nx, ny + 1, hi, lo, err)) return false;
+    if (!read_faces(p + "Z.dat", nx, ny, nz + 1, 1.0, fz, nx, ny, hi, lo, err)) return false;
+    return true;
+}
+
+bool read_n1(const std::string& path, int nx, int ny, int nz, std::vector<double>& n1, std::string& err) {
+    std::ifstream f(path);
+    if (!f) {
+        err = "No file " + path;
+        return false;
+    }
+    std::string header;
+    std::getline(f, header);
+    n1.assign((size_t)nx * ny * nz, 0.0);
+    float v;
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                if (!(f >> v)) {
+                    err = path + ": too few values";
+                    return false;
+                }
+                n1[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] = v;
+            }
+    return true;
+}
+
 }  // namespace nmr

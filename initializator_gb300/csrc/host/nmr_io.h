@@ -45,4 +45,13 @@ bool read_velocity(const std::string& dir, int nx, int ny, int nz, double vel_mu
                    std::vector<double>& vy, std::vector<double>& vz, double& vmax_raw, double& vmin_raw,
                    std::string& err);
 
+// SurfRel<key>{X,Y,Z}.dat, key one of 1Water 2Water 1Oil 2Oil (ReadSurfRel,
+// cpp:1035-1434): face arrays in the velocity layout, [k][j][i] with nx+1,
+// ny+1, nz+1 faces along the array's own axis
+bool read_surfrel(const std::string& dir, const std::string& key, int nx, int ny, int nz, std::vector<double>& fx,
+                  std::vector<double>& fy, std::vector<double>& fz, std::string& err);
+// n1_init.dat (cpp:974-1006): ik*jk*kk values read as float, i outer, k inner;
+// out [k][j][i]
+bool read_n1(const std::string& path, int nx, int ny, int nz, std::vector<double>& n1, std::string& err);
+
 }  // namespace nmr

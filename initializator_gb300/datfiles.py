@@ -13,6 +13,10 @@ consume identical inputs (reference ``src/NmrRelaxationSolve.cpp``):
 * ``Vx.dat`` / ``Vy.dat`` / ``Vz.dat`` — one header line, then (ik+1)*jk*kk,
   ik*(jk+1)*kk, ik*jk*(kk+1) doubles, i outermost, then j, then k
   (cpp:1466-1536); the solver multiplies them by VEL_MULT.
+* ``SurfRel{1,2}{Water,Oil}{X,Y,Z}.dat`` — face relaxivities in the layout of
+  the velocity files (cpp:1035-1434), read when nSurfRelWater / nSurfRelOil is 1.
+* ``n1_init.dat`` — one header line, then ik*jk*kk values read as float, i
+  outermost, then j, then k (cpp:974-1006): the first concentration of NCOMP 2.
 
 Array conventions of this package: ``mask[k, j, i]`` (1 = pore), face
 velocities ``vx[k, j, i]`` with i in [0, nx] (face i is the low face of cell i),
@@ -248,7 +252,45 @@ def read_velocity(dirpath: str, nx: int, ny: int, nz: int):
             np.ascontiguousarray(np.transpose(vz, t)))
 
 
-def write_case(dirpath: str, data: NmrData, mask: np.ndarray, vel=None, grads=(0.0,)) -> None:
+SURFREL_KEYS = ("1Water", "2Water", "1Oil", "2Oil")
+
+
+def write_surfrel(dirpath: str, key: str, fx: np.ndarray, fy: np.ndarray, fz: np.ndarray) -> None:
+    """Face relaxivities in this package's [k, j, i] face layout -> SurfRel<key>X/Y/Z.dat."""
+    for ax, a in zip("XYZ", (fx, fy, fz)):
+        _write_doubles(os.path.join(dirpath, f"SurfRel{key}{ax}.dat"), f"SurfRel{key}{ax}", np.transpose(a, (2, 1, 0)))
+
+
+def read_surfrel(dirpath: str, key: str, nx: int, ny: int, nz: int):
+    dims = {"X": (nx + 1, ny, nz), "Y": (nx, ny + 1, nz), "Z": (nx, ny, nz + 1)}
+    out = []
+    for ax in "XYZ":
+        n = int(np.prod(dims[ax]))
+        a = _read_doubles(os.path.join(dirpath, f"SurfRel{key}{ax}.dat"), n).reshape(dims[ax])
+        out.append(np.ascontiguousarray(np.transpose(a, (2, 1, 0))))
+    return tuple(out)
+
+
+def write_n1(path: str, n1: np.ndarray) -> None:
+    """n1[k, j, i] -> n1_init.dat (i outer, k inner), each value exactly a float."""
+    a = np.transpose(np.asarray(n1, dtype=np.float32), (2, 1, 0)).reshape(-1)
+    with open(path, "w") as f:
+        f.write("n1\n")
+        for x in a:
+            f.write(repr(float(x)) + "\n")
+
+
+def read_n1(path: str, nx: int, ny: int, nz: int) -> np.ndarray:
+    with open(path, "r") as f:
+        f.readline()
+        a = np.array(f.read().split(), dtype=np.float32)
+    if a.size < nx * ny * nz:
+        raise ValueError(f"{path}: expected {nx * ny * nz} values, found {a.size}")
+    return np.ascontiguousarray(np.transpose(a[: nx * ny * nz].reshape(nx, ny, nz), (2, 1, 0)))
+
+
+def write_case(dirpath: str, data: NmrData, mask: np.ndarray, vel=None, grads=(0.0,), surfrel=None,
+               n1=None) -> None:
     """Write a complete reference input directory (``dirpath/data/*.dat``)."""
     d = os.path.join(dirpath, "data")
     os.makedirs(d, exist_ok=True)
@@ -259,3 +301,7 @@ def write_case(dirpath: str, data: NmrData, mask: np.ndarray, vel=None, grads=(0
     write_poro(os.path.join(d, "Poro.dat"), mask)
     if vel is not None:
         write_velocity(d, *vel)
+    for key, faces in (surfrel or {}).items():
+        write_surfrel(d, key, *faces)
+    if n1 is not None:
+        write_n1(os.path.join(d, "n1_init.dat"), n1)

@@ -61,6 +61,12 @@ def lib():
         l.bto_run_reference.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p, dp, dp, dp, dp, dp, dp,
                                         ctypes.c_longlong, ctypes.POINTER(Pulse), ctypes.c_int, dp, dp, ctypes.c_int]
         l.bto_run_reference.restype = ctypes.c_int
+        l.bto_run_fields.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p, dp, dp, dp, dp, dp, dp,
+                                     ctypes.c_longlong, ctypes.POINTER(Pulse), ctypes.c_int, dp, dp, dp, dp, dp, dp,
+                                     dp, dp, ctypes.c_int]
+        l.bto_run_fields.restype = ctypes.c_int
+        l.bto_run_maccormack.argtypes = l.bto_run_fields.argtypes
+        l.bto_run_maccormack.restype = ctypes.c_int
         l.bto_sums.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p, dp, dp, dp, dp]
         l.bto_sums.restype = ctypes.c_longlong
         l.bto_rates.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p, dp, dp]
@@ -93,8 +99,15 @@ def make_params(shape, *, dx, dy=None, dz=None, dt, main_field=(1.0, 0.0, 0.0), 
     return p
 
 
-def run(params: Params, mask, state, nsteps, vel=None, pulses=(), grad_wave=None, threads=0):
-    """Advance ``state`` (3, nz, ny, nx) float64 by nsteps; returns (state, mt[nsteps, 3])."""
+def run(params: Params, mask, state, nsteps, vel=None, pulses=(), grad_wave=None, threads=0, fields=None,
+        phases=None, maccormack=False):
+    """Advance ``state`` (3, nz, ny, nx) float64 by nsteps; returns (state, mt[nsteps, 3]).
+
+    fields = (t1, t2, diff): per-voxel coefficients replacing the uniform
+    fluid's (dense (nz, ny, nx)). phases = (c1, c2): phase fractions; then the
+    return value is (state, mt, mt6[nsteps, 6]) with the two-component sums.
+    maccormack: the reference's GPU scheme (predictor-corrector) instead of
+    ExplicitSimple."""
     mask = np.ascontiguousarray(mask, dtype=np.uint8)
     st = np.array(state, dtype=np.float64, copy=True)
     mx, my, mz = (np.ascontiguousarray(st[c]) for c in range(3))
@@ -107,11 +120,24 @@ def run(params: Params, mask, state, nsteps, vel=None, pulses=(), grad_wave=None
         parr[n].axis[:] = list(axis)
     gw = None if grad_wave is None else np.ascontiguousarray(grad_wave, dtype=np.float64)
     mt = np.zeros((max(nsteps, 1), 3), dtype=np.float64)
-    rc = lib().bto_run_reference(ctypes.byref(params), mask.ctypes.data, _dp(vx), _dp(vy), _dp(vz),
-                                 _dp(mx), _dp(my), _dp(mz), nsteps, parr, len(pulses), _dp(gw), _dp(mt), threads)
+    if fields is None and phases is None and not maccormack:
+        rc = lib().bto_run_reference(ctypes.byref(params), mask.ctypes.data, _dp(vx), _dp(vy), _dp(vz),
+                                     _dp(mx), _dp(my), _dp(mz), nsteps, parr, len(pulses), _dp(gw), _dp(mt), threads)
+        if rc != 0:
+            raise RuntimeError(f"oracle failed: {rc}")
+        return np.stack([mx, my, mz]), mt[:nsteps]
+    f = [None, None, None] if fields is None else [np.ascontiguousarray(a, dtype=np.float64) for a in fields]
+    c = [None, None] if phases is None else [np.ascontiguousarray(a, dtype=np.float64) for a in phases]
+    mt6 = None if phases is None else np.zeros((max(nsteps, 1), 6), dtype=np.float64)
+    fn = lib().bto_run_maccormack if maccormack else lib().bto_run_fields
+    rc = fn(ctypes.byref(params), mask.ctypes.data, _dp(vx), _dp(vy), _dp(vz),
+                              _dp(mx), _dp(my), _dp(mz), nsteps, parr, len(pulses), _dp(gw),
+                              _dp(f[0]), _dp(f[1]), _dp(f[2]), _dp(c[0]), _dp(c[1]), _dp(mt), _dp(mt6), threads)
     if rc != 0:
         raise RuntimeError(f"oracle failed: {rc}")
-    return np.stack([mx, my, mz]), mt[:nsteps]
+    if phases is None:
+        return np.stack([mx, my, mz]), mt[:nsteps]
+    return np.stack([mx, my, mz]), mt[:nsteps], mt6[:nsteps]
 
 
 def last_loop_seconds() -> float:

@@ -272,6 +272,99 @@ static void update_plane(const bto_params* p, const ofields_t* f, int k, const d
     }
 }
 
+/* One stage of the reference's GPU scheme, MacCormack predictor-corrector
+ * (ExplicitMakUpgrade cu:1473-1498): stage 0 = NMR_predictor_upgrade
+ * (cu:637-801) from the field M into P, stage 1 = NMR_corrector_upgrade
+ * (cu:803-967) from P into the corrected field. Relaxation, cross product and
+ * diffusion (face diffusivity 2DaDb/(Da+Db+1e-25)) act on the stage's input;
+ * advection uses the cell-average velocity with backward differences in the
+ * predictor and forward differences in the corrector. A solid neighbour in an
+ * advective difference holds the voxel's own value (the reference writes it
+ * there first; with several writers the GPU's pick is racy, this is the
+ * zero-flux reading). Corrector: out = 0.5 * (M + P + the terms of P), summed
+ * in the reference's order. */
+static void mac_plane(const bto_params* p, const ofields_t* f, int k, const double G[3], int stage,
+                      const double* iX, const double* iY, const double* iZ, double* oX, double* oY, double* oZ) {
+    const grid_t* g = &f->g;
+    const double dTime = p->dt;
+    const double hx = dTime / p->dx, hy = dTime / p->dy, hz = dTime / p->dz;
+    const double hxx = dTime / (p->dx * p->dx), hyy = dTime / (p->dy * p->dy), hzz = dTime / (p->dz * p->dz);
+    const double* D = f->D;
+    const double Bx = p->main_field[0], By = p->main_field[1], Bz = p->main_field[2];
+    const double reg = 1.0e-25;
+    const int km = k - 1, kp = k + 1;
+    for (int j = 1; j <= g->ny; j++) {
+        const int jm = j - 1, jp = j + 1;
+        for (int i = 1; i <= g->nx; i++) {
+            const int im = i - 1, ip = i + 1;
+            const size_t c = gidx(g, i, j, k);
+            if (f->act[c] != 1) continue;
+            const size_t cxp = gidx(g, ip, j, k), cxm = gidx(g, im, j, k);
+            const size_t cyp = gidx(g, i, jp, k), cym = gidx(g, i, jm, k);
+            const size_t czp = gidx(g, i, j, kp), czm = gidx(g, i, j, km);
+            const double* in[3] = {iX, iY, iZ};
+            const double p0[3] = {iX[c], iY[c], iZ[c]};
+            const double tau1 = 1.0 / f->t1[c];
+            const double tau2 = 1.0 / f->t2[c];
+            const double anb = sqrt(Bx * Bx + By * By + Bz * Bz);
+            const double an[3] = {Bx / anb, By / anb, Bz / anb};
+            const double pEq = p->p_eq;
+            const double div = an[0] * p0[0] + an[1] * p0[1] + an[2] * p0[2];
+            const double b = dTime * 4.78941714e+7;
+            const double bb[3] = {b * (G[0] * p->dx * ((double)i - 0.5)), b * (G[1] * p->dy * ((double)j - 0.5)),
+                                  b * (G[2] * p->dz * ((double)k - 0.5))};
+            double dxp = 0, dxm = 0, dyp = 0, dym = 0, dzp = 0, dzm = 0;
+            if (p->diffusion == 1) {
+                dxp = 2.0 * (D[cxp] * D[c]) / (D[cxp] + D[c] + reg);
+                dxm = 2.0 * (D[cxm] * D[c]) / (D[cxm] + D[c] + reg);
+                dyp = 2.0 * (D[cyp] * D[c]) / (D[cyp] + D[c] + reg);
+                dym = 2.0 * (D[cym] * D[c]) / (D[cym] + D[c] + reg);
+                dzp = 2.0 * (D[czp] * D[c]) / (D[czp] + D[c] + reg);
+                dzm = 2.0 * (D[czm] * D[c]) / (D[czm] + D[c] + reg);
+            }
+            double u = 0, v = 0, w = 0;
+            if (p->velocity == 1) {
+                u = 0.5 * (f->vx[c] + f->vx[cxp]);
+                v = 0.5 * (f->vy[c] + f->vy[cyp]);
+                w = 0.5 * (f->vz[c] + f->vz[czp]);
+            }
+            const double* mold[3] = {f->mx, f->my, f->mz};
+            double* out[3] = {oX, oY, oZ};
+            for (int a = 0; a < 3; a++) {
+                const double* m = in[a];
+                const double pa = p0[a];
+                const double diva = an[a] * div;
+                const double rel = dTime * tau1 * (pEq * an[a] - diva) + dTime * tau2 * (diva - pa);
+                double vec = 0.0;
+                if (p->vector_mult == 1) {
+                    if (a == 0) vec = 0.0 - bb[1] * p0[2] + bb[2] * p0[1];
+                    if (a == 1) vec = 0.0 + bb[0] * p0[2] - bb[2] * p0[0];
+                    if (a == 2) vec = 0.0 - bb[0] * p0[1] + bb[1] * p0[0];
+                }
+                double dif = 0.0;
+                if (p->diffusion == 1)
+                    dif = hxx * (dxp * (m[cxp] - pa) - dxm * (pa - m[cxm]))
+                        + hyy * (dyp * (m[cyp] - pa) - dym * (pa - m[cym]))
+                        + hzz * (dzp * (m[czp] - pa) - dzm * (pa - m[czm]));
+                double vel = 0.0;
+                if (p->velocity == 1) {
+                    if (stage == 0) {
+                        const double xm = f->act[cxm] ? m[cxm] : pa, ym = f->act[cym] ? m[cym] : pa;
+                        const double zm = f->act[czm] ? m[czm] : pa;
+                        vel = 0.0 - u * hx * (pa - xm) - v * hy * (pa - ym) - w * hz * (pa - zm);
+                    } else {
+                        const double xp = f->act[cxp] ? m[cxp] : pa, yp = f->act[cyp] ? m[cyp] : pa;
+                        const double zp = f->act[czp] ? m[czp] : pa;
+                        vel = 0.0 - u * hx * (xp - pa) - v * hy * (yp - pa) - w * hz * (zp - pa);
+                    }
+                }
+                if (stage == 0) out[a][c] = pa + rel + vec + dif + vel;
+                else out[a][c] = 0.5 * (mold[a][c] + pa + rel + vec + dif + vel);
+            }
+        }
+    }
+}
+
 /* OrtTransform (cpp:2536-2550): Rodrigues rotation of one voxel */
 static inline void ort(double* x, double* y, double* z, double nx, double ny, double nz, double angle) {
     double c = cos(angle), s = sin(angle);
@@ -374,12 +467,35 @@ static long long field_sums(const bto_params* p, const grid_t* g, const char* ac
     return count;
 }
 
-int bto_run_reference(const bto_params* p, const uint8_t* mask,
-                      const double* vx, const double* vy, const double* vz,
-                      double* mx, double* my, double* mz,
-                      long long nsteps, const bto_pulse* pulses, int npulses,
-                      const double* grad_wave, double* mt, int threads) {
+/* OutputX/Y/Z with two components (cpp:3324-3350): over pore voxels of the
+ * trimming box where c1 > 0.8 or c2 > 0.8, sum_1 += M * c1 and sum_2 += M * c2,
+ * k outer, j, i inner. out = {x1, y1, z1, x2, y2, z2}. c1, c2 dense. */
+static void phase_sums(const bto_params* p, const grid_t* g, const char* act, const double* c1, const double* c2,
+                       const double* mx, const double* my, const double* mz, double* out) {
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = 1 + p->buffer[2]; k < g->nz + 1 - p->buffer[2]; k++)
+        for (int j = 1 + p->buffer[1]; j < g->ny + 1 - p->buffer[1]; j++)
+            for (int i = 1 + p->buffer[0]; i < g->nx + 1 - p->buffer[0]; i++) {
+                size_t c = gidx(g, i, j, k);
+                if (act[c] != 1) continue;
+                size_t q = (size_t)(i - 1) + (size_t)g->nx * ((size_t)(j - 1) + (size_t)g->ny * (k - 1));
+                if (!(c1[q] > 0.8 || c2[q] > 0.8)) continue;
+                s[0] += mx[c] * c1[q]; s[3] += mx[c] * c2[q];
+                s[1] += my[c] * c1[q]; s[4] += my[c] * c2[q];
+                s[2] += mz[c] * c1[q]; s[5] += mz[c] * c2[q];
+            }
+    for (int a = 0; a < 6; a++) out[a] = s[a];
+}
+
+static int run_impl(const bto_params* p, const uint8_t* mask,
+                    const double* vx, const double* vy, const double* vz,
+                    double* mx, double* my, double* mz,
+                    long long nsteps, const bto_pulse* pulses, int npulses,
+                    const double* grad_wave, const double* t1, const double* t2, const double* diff,
+                    const double* c1, const double* c2, double* mt, double* mt6, int threads, int maccormack) {
     if (!p || p->nx <= 0 || p->ny <= 0 || p->nz <= 0 || nsteps < 0) return -1;
+    if ((t1 || t2 || diff) && !(t1 && t2 && diff)) return -1;
+    if (mt6 && !(c1 && c2)) return -1;
 #ifdef _OPENMP
     int saved = omp_get_max_threads();
     if (threads > 0) omp_set_num_threads(threads);
@@ -388,14 +504,46 @@ int bto_run_reference(const bto_params* p, const uint8_t* mask,
 #endif
     ofields_t f;
     if (ofields_init(p, mask, vx, vy, vz, mx, my, mz, &f)) return -2;
+    if (t1) {
+        /* the caller's FillInDiffusinAndTime fields replace the uniform fluid's */
+        for (int k = 0; k < p->nz; k++)
+            for (int j = 0; j < p->ny; j++)
+                for (int i = 0; i < p->nx; i++) {
+                    size_t s = (size_t)i + (size_t)p->nx * ((size_t)j + (size_t)p->ny * k);
+                    size_t c = gidx(&f.g, i + 1, j + 1, k + 1);
+                    f.t1[c] = t1[s]; f.t2[c] = t2[s]; f.D[c] = diff[s];
+                }
+        bc_copy_d(&f.g, f.D);
+    }
     double* scratch = (double*)calloc((size_t)3 * (p->nz + 2), sizeof(double));
     const grid_t* g = &f.g;
+    /* MacCormack: the corrector's output (zero in solid and ghosts) */
+    double *cx = NULL, *cy = NULL, *cz = NULL;
+    if (maccormack) {
+        cx = (double*)calloc(g->num, sizeof(double));
+        cy = (double*)calloc(g->num, sizeof(double));
+        cz = (double*)calloc(g->num, sizeof(double));
+    }
     const double t_start = now_s();
     for (long long s = 0; s < nsteps; s++) {
         double G[3] = {p->grad[0], p->grad[1], p->grad[2]};
         if (grad_wave) { G[0] = grad_wave[3 * s]; G[1] = grad_wave[3 * s + 1]; G[2] = grad_wave[3 * s + 2]; }
-        #pragma omp parallel for schedule(static)
-        for (int k = 1; k <= g->nz; k++) update_plane(p, &f, k, G);
+        if (maccormack) {
+            /* predictor into the add arrays (zero in solid), copy ghosts, then
+             * the corrector from it into P's partner; M = the corrected field */
+            #pragma omp parallel for schedule(static)
+            for (size_t q = 0; q < g->num; q++) { f.ax[q] = 0.0; f.ay[q] = 0.0; f.az[q] = 0.0; }
+            #pragma omp parallel for schedule(static)
+            for (int k = 1; k <= g->nz; k++) mac_plane(p, &f, k, G, 0, f.mx, f.my, f.mz, f.ax, f.ay, f.az);
+            bc_copy_d(g, f.ax); bc_copy_d(g, f.ay); bc_copy_d(g, f.az);
+            #pragma omp parallel for schedule(static)
+            for (int k = 1; k <= g->nz; k++) mac_plane(p, &f, k, G, 1, f.ax, f.ay, f.az, cx, cy, cz);
+            #pragma omp parallel for schedule(static)
+            for (size_t q = 0; q < g->num; q++) { f.ax[q] = cx[q]; f.ay[q] = cy[q]; f.az[q] = cz[q]; }
+        } else {
+            #pragma omp parallel for schedule(static)
+            for (int k = 1; k <= g->nz; k++) update_plane(p, &f, k, G);
+        }
         /* copy the interior back (cpp:3269-3280); solid voxels take the add
          * arrays' untouched value, which is zero */
         #pragma omp parallel for schedule(static)
@@ -411,6 +559,7 @@ int bto_run_reference(const bto_params* p, const uint8_t* mask,
             if (pulses[q].step == s) add_impulse(p, &f, &pulses[q]);
         bc_copy_d(g, f.mx); bc_copy_d(g, f.my); bc_copy_d(g, f.mz);
         if (mt) field_sums(p, g, f.act, f.mx, f.my, f.mz, &mt[3 * s], scratch);
+        if (mt6) phase_sums(p, g, f.act, c1, c2, f.mx, f.my, f.mz, &mt6[6 * s]);
     }
     g_loop_seconds = now_s() - t_start;
     for (int k = 0; k < p->nz; k++)
@@ -421,11 +570,41 @@ int bto_run_reference(const bto_params* p, const uint8_t* mask,
                 mx[s] = f.mx[c]; my[s] = f.my[c]; mz[s] = f.mz[c];
             }
     free(scratch);
+    free(cx); free(cy); free(cz);
     ofields_free(&f);
 #ifdef _OPENMP
     omp_set_num_threads(saved);
 #endif
     return 0;
+}
+
+int bto_run_reference(const bto_params* p, const uint8_t* mask,
+                      const double* vx, const double* vy, const double* vz,
+                      double* mx, double* my, double* mz,
+                      long long nsteps, const bto_pulse* pulses, int npulses,
+                      const double* grad_wave, double* mt, int threads) {
+    return run_impl(p, mask, vx, vy, vz, mx, my, mz, nsteps, pulses, npulses, grad_wave, NULL, NULL, NULL, NULL,
+                    NULL, mt, NULL, threads, 0);
+}
+
+int bto_run_fields(const bto_params* p, const uint8_t* mask,
+                   const double* vx, const double* vy, const double* vz,
+                   double* mx, double* my, double* mz,
+                   long long nsteps, const bto_pulse* pulses, int npulses, const double* grad_wave,
+                   const double* t1, const double* t2, const double* diff,
+                   const double* c1, const double* c2, double* mt, double* mt6, int threads) {
+    return run_impl(p, mask, vx, vy, vz, mx, my, mz, nsteps, pulses, npulses, grad_wave, t1, t2, diff, c1, c2, mt,
+                    mt6, threads, 0);
+}
+
+int bto_run_maccormack(const bto_params* p, const uint8_t* mask,
+                       const double* vx, const double* vy, const double* vz,
+                       double* mx, double* my, double* mz,
+                       long long nsteps, const bto_pulse* pulses, int npulses, const double* grad_wave,
+                       const double* t1, const double* t2, const double* diff,
+                       const double* c1, const double* c2, double* mt, double* mt6, int threads) {
+    return run_impl(p, mask, vx, vy, vz, mx, my, mz, nsteps, pulses, npulses, grad_wave, t1, t2, diff, c1, c2, mt,
+                    mt6, threads, 1);
 }
 
 long long bto_sums(const bto_params* p, const uint8_t* mask,

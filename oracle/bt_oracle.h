@@ -57,6 +57,31 @@ int bto_run_reference(const bto_params* p, const uint8_t* mask,
                       long long nsteps, const bto_pulse* pulses, int npulses,
                       const double* grad_wave, double* mt, int threads);
 
+/* bto_run_reference with per-voxel coefficients and two-component sums.
+ * t1, t2 (s) and diff (m^2/s): dense [nz][ny][nx] arrays that replace what
+ * FillInDiffusinAndTime forms for the uniform fluid (all NULL: the fluid of p).
+ * c1, c2: dense phase fractions; with mt6 non-NULL, mt6 receives 6*nsteps sums
+ * {x1, y1, z1, x2, y2, z2} after each step (OutputX/Y/Z with NCOMP 2,
+ * NmrRelaxationSolve.cpp:3324-3350). */
+int bto_run_fields(const bto_params* p, const uint8_t* mask,
+                   const double* vx, const double* vy, const double* vz,
+                   double* mx, double* my, double* mz,
+                   long long nsteps, const bto_pulse* pulses, int npulses, const double* grad_wave,
+                   const double* t1, const double* t2, const double* diff,
+                   const double* c1, const double* c2, double* mt, double* mt6, int threads);
+
+/* bto_run_fields with the reference's GPU scheme (solve_gpu's
+ * ExplicitMakUpgrade, NmrRelaxationSolveKernels.cu:1473-1498): MacCormack
+ * predictor (backward-difference advection, cu:637-801), copy ghosts,
+ * corrector (forward differences, 0.5 * (M + P + terms), cu:803-967) per step.
+ * vector_mult 2 is not available in this scheme. */
+int bto_run_maccormack(const bto_params* p, const uint8_t* mask,
+                       const double* vx, const double* vy, const double* vz,
+                       double* mx, double* my, double* mz,
+                       long long nsteps, const bto_pulse* pulses, int npulses, const double* grad_wave,
+                       const double* t1, const double* t2, const double* diff,
+                       const double* c1, const double* c2, double* mt, double* mt6, int threads);
+
 /* Wall time (s) of the stepping loop of the last bto_run_reference call. */
 double bto_last_loop_seconds(void);
 

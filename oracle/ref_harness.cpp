@@ -18,7 +18,9 @@
 //   AddImpulse calls replace Sequence() (so every pulse flag can be pinned).
 // outputs in outdir: mt.bin ((nsteps+1)*3 doubles, sums before each step and
 //   after the last), state.bin (3*N doubles), rates.bin (tau1 then tau2, N each),
-//   diff.bin (N), info.txt.
+//   times.bin (relTime.t1 then relTime.t2 as stored, N each), diff.bin (N),
+//   info.txt; with NCOMP 2 also mt6.bin ((nsteps+1)*6 doubles: X1 Y1 Z1 X2 Y2 Z2)
+//   and phases.bin (the concentrations, 2*N).
 
 // standard headers first, so that the access override below only reaches the
 // reference's class
@@ -104,11 +106,17 @@ int main(int argc, char** argv) {
                 }
         s.BoundaryConditionsForVectorField(&s.magnetization);
     }
-    std::vector<double> mt;
+    std::vector<double> mt, mt6;
+    auto push6 = [&]() {
+        if (s.nComponents != 2) return;
+        const double v6[6] = {s.resX1, s.resY1, s.resZ1, s.resX2, s.resY2, s.resZ2};
+        mt6.insert(mt6.end(), v6, v6 + 6);
+    };
     for (long i = 0; i < nsteps; i++) {
         s.currentTime = i * s.dTime;
         s.OutputX(&s.magnetization); s.OutputY(&s.magnetization); s.OutputZ(&s.magnetization);
         mt.push_back(s.resX); mt.push_back(s.resY); mt.push_back(s.resZ);
+        push6();
         s.ExplicitSimple();
         if (explicit_pulses) {
             for (const Pulse& p : pulses)
@@ -120,8 +128,9 @@ int main(int argc, char** argv) {
     }
     s.OutputX(&s.magnetization); s.OutputY(&s.magnetization); s.OutputZ(&s.magnetization);
     mt.push_back(s.resX); mt.push_back(s.resY); mt.push_back(s.resZ);
+    push6();
 
-    std::vector<double> st(3 * N), rates(2 * N), diff(N);
+    std::vector<double> st(3 * N), rates(2 * N), times(2 * N), diff(N), phases(2 * N);
     for (int k = 0; k < gs.kk; k++)
         for (int j = 0; j < gs.jk; j++)
             for (int i = 0; i < gs.ik; i++) {
@@ -132,12 +141,21 @@ int main(int argc, char** argv) {
                 st[2 * N + q] = s.magnetization.z[c];
                 rates[q] = 1.0 / s.relTime.t1[c];
                 rates[N + q] = 1.0 / s.relTime.t2[c];
+                times[q] = s.relTime.t1[c];
+                times[N + q] = s.relTime.t2[c];
                 diff[q] = s.diffusion[c];
+                phases[q] = s.concentration[0][c];
+                phases[N + q] = s.concentration[1][c];
             }
     dump(outdir + "/mt.bin", mt.data(), mt.size());
     dump(outdir + "/state.bin", st.data(), st.size());
     dump(outdir + "/rates.bin", rates.data(), rates.size());
     dump(outdir + "/diff.bin", diff.data(), diff.size());
+    dump(outdir + "/times.bin", times.data(), times.size());
+    if (s.nComponents == 2) {
+        dump(outdir + "/mt6.bin", mt6.data(), mt6.size());
+        dump(outdir + "/phases.bin", phases.data(), phases.size());
+    }
     FILE* f = std::fopen((outdir + "/info.txt").c_str(), "w");
     std::fprintf(f, "nx %d\nny %d\nnz %d\ndTime %.17g\npEq %.17g\nnStep %d\ndirection %.17g %.17g %.17g\n",
                  gs.ik, gs.jk, gs.kk, s.dTime, s.equilibriumMagnetization, s.nStep,

@@ -21,7 +21,11 @@ def write_case_dir(case, path):
           for f in dataclasses.fields(datfiles.NmrData)}
     data = datfiles.NmrData(**kw)
     vel = (z["vx"], z["vy"], z["vz"]) if data.n_velocity == 1 else None
-    datfiles.write_case(path, data, z["mask"], vel=vel, grads=tuple(z["grads"]))
+    surf = {}
+    for key in datfiles.SURFREL_KEYS:
+        if f"surf_{key}_x" in z:
+            surf[key] = tuple(z[f"surf_{key}_{ax}"] for ax in "xyz")
+    datfiles.write_case(path, data, z["mask"], vel=vel, grads=tuple(z["grads"]), surfrel=surf, n1=z.get("n1"))
     return z
 
 
@@ -36,8 +40,11 @@ def build_driver():
     return DRIVER
 
 
-def describe(path):
-    out = subprocess.run([build_driver(), path], capture_output=True, text=True, check=True).stdout
+def describe(path, fields_out=None):
+    """What the drop-in's init() derived; with fields_out, also its per-voxel
+    T1, T2, D, c1, c2 arrays (5 x N doubles) written to that file."""
+    args = [build_driver(), path] + (["--fields", fields_out] if fields_out else [])
+    out = subprocess.run(args, capture_output=True, text=True, check=True).stdout
     vals = {}
     for line in out.split("BEGIN-DESCRIBE\n", 1)[1].splitlines():
         k, *v = line.split()

@@ -75,3 +75,19 @@ def test_schedule_maps_to_coarse_steps():
     assert cg.coarse_pulses([(7, 2, 3.14, (1, 0, 0))]) == [(1, 2, 3.14, (1, 0, 0))]
     with pytest.raises(ValueError):
         cg.coarse_pulses([(6, 2, 3.14, (1, 0, 0))])
+
+
+def test_pore_average_restriction_keeps_weighted_lab_sums():
+    rng = np.random.default_rng(2)
+    mask = (rng.random((6, 4, 8)) > 0.4).astype(np.uint8)
+    f = [torch.tensor(rng.standard_normal((6, 4, 8)) * mask) for _ in range(3)]
+    k = np.array([3e5, -2e5, 1e5])
+    dxf = (1e-6,) * 3
+    c = cg.restrict(f, k, dxf, mask)
+    _, phi, _ = cg.coarsen_geometry(mask, None)
+    a = cg.lab_sums(f, k, dxf)
+    b = 8 * cg.lab_sums(c, k, (2e-6,) * 3, phi)
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+    back = cg.restrict(cg.prolong(c, k, dxf, mask, pore_average=True), k, dxf, mask)
+    for x, y in zip(c, back):
+        assert float((x - y).abs().max()) < 1e-14

@@ -29,6 +29,25 @@ def test_init_matches_reference(case, tmp_path, btlib):
     assert d["gradientPulse"][0] == z["gradient_pulse"]
 
 
+@pytest.mark.parametrize("case", ["surfrel", "two_phase"])
+def test_init_fields_match_reference(case, tmp_path, btlib):
+    """SurfRel*.dat and n1_init.dat read by the drop-in: its per-voxel T1, T2,
+    D are the reference's relTime / diffusion arrays bit for bit, and its time
+    step matches the reference's init()."""
+    from test_fluid_golden import coeffs
+    z = write_case_dir(case, str(tmp_path / "case"))
+    out = str(tmp_path / "fields.bin")
+    d = describe(str(tmp_path / "case"), fields_out=out)
+    n = z["mask"].size
+    f = np.fromfile(out).reshape(5, *z["mask"].shape)
+    assert np.array_equal(f[0], z["t1f"]) and np.array_equal(f[1], z["t2f"]) and np.array_equal(f[2], z["diff"])
+    _, (p1, p2), _ = coeffs(z)
+    assert np.array_equal(f[3], p1) and np.array_equal(f[4], p2)
+    assert abs(d["dTime"][0] / z["dt_init"] - 1) <= 1e-14
+    assert int(d["nStep"][0]) == int(z["nstep_init"])
+    assert n == f[0].size
+
+
 def _read_csv(path):
     rows = []
     with open(path) as f:
@@ -38,13 +57,24 @@ def _read_csv(path):
     return np.array(rows)
 
 
+def _phase_sums0(z, st0, p1, p2):
+    """OutputX/Y/Z with two components (cpp:3324-3350) of a field."""
+    bx, by, bz = int(z["data_buffer_x"]), int(z["data_buffer_y"]), int(z["data_buffer_z"])
+    nz, ny, nx = z["mask"].shape
+    sel = np.zeros(z["mask"].shape, bool)
+    sel[bz:nz - bz, by:ny - by, bx:nx - bx] = True
+    sel &= (z["mask"] == 1) & ((p1 > 0.8) | (p2 > 0.8))
+    return np.array([(st0[c] * p1)[sel].sum() for c in range(3)] + [(st0[c] * p2)[sel].sum() for c in range(3)])
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["fid", "pfg_flow"])
+@pytest.mark.parametrize("case", ["fid", "pfg_flow", "surfrel", "two_phase"])
 @pytest.mark.parametrize("path", ["gpu", "cpu"])
 def test_nmr_exe_end_to_end(case, path, tmp_path, btlib, oracle_lib):
     import initializator_gb300 as bt
     import oracle
     from initializator_gb300 import build
+    from test_fluid_golden import coeffs
     z = write_case_dir(case, str(tmp_path))
     d = describe(str(tmp_path))
     env = dict(os.environ)
@@ -63,12 +93,18 @@ def test_nmr_exe_end_to_end(case, path, tmp_path, btlib, oracle_lib):
                               gradient_pulse=float(z["gradient_pulse"]), gpu_variant=(path == "gpu"))
     p = oracle.make_params(z["mask"].shape, **kw)
     st0 = initial_state(z)
-    s0, _ = oracle.sums(p, z["mask"], st0)
-    _, mt = oracle.run(p, z["mask"], st0, nstep + 1, vel=velocity(z), pulses=pl)
+    two = int(z["data_n_components"]) == 2
+    per_voxel = two or int(z["data_n_surf_rel_water"]) == 1 or int(z["data_n_surf_rel_oil"]) == 1
+    _, (p1, p2), _ = coeffs(z)
+    fields = (z["t1f"], z["t2f"], z["diff"]) if per_voxel else None
+    res = oracle.run(p, z["mask"], st0, nstep + 1, vel=velocity(z), pulses=pl, fields=fields,
+                     phases=(p1, p2) if two else None)
+    mt = res[2] if two else res[1]
+    s0 = _phase_sums0(z, st0, p1, p2) if two else oracle.sums(p, z["mask"], st0)[0]
     nd = int(z["data_nd_print"])
     steps = np.arange(0, nstep + 1, nd)
     ref = mt[steps] if path == "gpu" else np.vstack([s0[None], mt])[steps]
-    assert got.shape == (len(steps), 4)
+    assert got.shape == (len(steps), 7 if two else 4)
     assert np.allclose(got[:, 0], steps * dt, rtol=5e-6)
     scale = np.abs(ref).max()
     assert np.abs(got[:, 1:] - ref).max() <= 5e-6 * scale

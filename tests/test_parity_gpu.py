@@ -339,3 +339,64 @@ def test_ragged_batch_matches_single_runs(btlib):
     ref, ref_mt = oracle.run(p, mask, st0, n, vel=vel, pulses=rf, grad_wave=wave)
     assert rel_err(states[1], ref) <= KS64_TOL
     assert rel_err(mts[1], ref_mt) <= KS64_TOL
+
+
+@pytest.mark.parametrize("case", ["surfrel", "two_phase"])
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_per_voxel_fields_match_reference(case, precision, btlib):
+    """SurfRel face relaxivities and two-component fluids: the reference's own
+    relTime / diffusion arrays uploaded per voxel. FP64: field bit-identical,
+    M(t) (one-component sums, or the six two-component sums) within 1e-12;
+    FP32: M(t) within 1e-4."""
+    import initializator_gb300 as bt
+    from test_fluid_golden import coeffs
+    z = load(case)
+    two = int(z["data_n_components"]) == 2
+    prec = bt.BT_F64 if precision == "f64" else bt.BT_F32
+    _, (p1, p2), _ = coeffs(z)
+    n = int(z["nsteps"])
+    with _solver(z, prec) as s:
+        s.upload_rates(z["t1f"], z["t2f"], z["diff"])
+        if two:
+            s.set_phase_weights(p1, p2)
+        s.set_state(initial_state(z))
+        s.set_schedule(pulses(z))
+        mt = s.run(n)
+        st = s.get_state()
+        mt6 = s.read_mt_phases(n) if two else None
+    tol = F64_TOL if precision == "f64" else F32_MT_TOL
+    if precision == "f64":
+        assert np.array_equal(st, z["state"]), f"max abs diff {np.abs(st - z['state']).max()}"
+    if two:
+        assert rel_err(mt6, z["mt6"][1:]) <= tol
+    else:
+        assert rel_err(mt, z["mt"][1:]) <= tol
+
+
+def test_per_voxel_fields_reset_and_tma_skip(btlib):
+    """Uploading the reference's coefficient arrays of a uniform-fluid case
+    per voxel reproduces the code-table path bit for bit (FP64) and through
+    the generic kernel in FP32 (the TMA path is skipped), and NULL returns to
+    the code tables."""
+    import initializator_gb300 as bt
+    z = load("pfg_flow")
+    for prec in (bt.BT_F64, bt.BT_F32):
+        with _solver(z, prec) as s:
+            s.set_state(initial_state(z))
+            s.set_schedule(pulses(z))
+            ref = s.run(20)
+            ref_st = s.get_state()
+        with _solver(z, prec) as s:
+            s.upload_rates(z["t1f"], z["t2f"], z["diff"])
+            s.set_state(initial_state(z))
+            s.set_schedule(pulses(z))
+            mt = s.run(20)
+            if prec == bt.BT_F64:
+                assert np.array_equal(s.get_state(), ref_st)
+                assert np.array_equal(mt, ref)
+            else:
+                assert rel_err(mt, ref) <= 1e-6
+            s.upload_rates()
+            s.set_state(initial_state(z))
+            s.set_step(0)
+            assert np.array_equal(s.run(20), ref)
