@@ -803,7 +803,10 @@ int run_advance(bt_handle* h, long long* s, long long end, long long limit) {
                 CK(h, e);
             }
             CK(h, cudaGraphLaunch(g, h->stream));
-            h->launches += GRAPH_STEPS;
+            // kernels per step: the step (two for MacCormack) and, with
+            // two-component sums, their two reduction kernels
+            const int per_step = (h->cfg.scheme == BT_SCHEME_MACCORMACK ? 2 : 1) + (h->weights_d ? 2 : 0);
+            h->launches += (long long)GRAPH_STEPS * per_step;
             *s += GRAPH_STEPS;
         } else {
             CK(h, launch_one(h, h->cur, *s));

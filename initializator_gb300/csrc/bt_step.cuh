@@ -126,19 +126,13 @@ __device__ __forceinline__ void lab_phase(double k, int c, double d, T& re, T& i
 // the result does not depend on scheduling), writes M(t), checks it for
 // NaN/Inf and advances the device step counter. red: >= 3 doubles per warp;
 // flag: one shared int.
+// the part after each warp's lane 0 has written its 3 sums to red
 template <typename T>
-__device__ __forceinline__ void finish_step(const StepParams<T>& P, long long step, unsigned b, unsigned local,
-                                            unsigned nb_per, double s[3], double* red, int* flag) {
+__device__ __forceinline__ void finish_step_red(const StepParams<T>& P, long long step, unsigned b, unsigned local,
+                                                unsigned nb_per, double* red, int* flag) {
     const int nthreads = blockDim.x * blockDim.y;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int lane = tid & 31, warp = tid >> 5, nwarps = nthreads / 32;
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
-    if (lane == 0)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) red[warp * 3 + c] = s[c];
     __syncthreads();
     const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
     if (tid == 0) {
@@ -193,6 +187,52 @@ __device__ __forceinline__ void finish_step(const StepParams<T>& P, long long st
         P.ctl->step = step + 1;
         __threadfence();
     }
+}
+
+template <typename T>
+__device__ __forceinline__ void finish_step(const StepParams<T>& P, long long step, unsigned b, unsigned local,
+                                            unsigned nb_per, double s[3], double* red, int* flag) {
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) red[warp * 3 + c] = s[c];
+    finish_step_red<T>(P, step, b, local, nb_per, red, flag);
+}
+
+// s + e = a + b exactly (Knuth's TwoSum, FP32)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// FP32 path: the warp-level reduction of the Kahan sums as float-float pairs
+// (hi + lo, TwoSum per step) instead of FP64, whose pipe is narrow on this
+// part; each warp's pair becomes one FP64 partial at lane 0
+__device__ __forceinline__ void finish_step_acc(const StepParams<float>& P, long long step, unsigned b, unsigned local,
+                                                unsigned nb_per, const Acc<float> (&acc)[3], double* red, int* flag) {
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float h = acc[c].s, l = -acc[c].c;  // Acc holds s - c
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float bh = __shfl_down_sync(0xffffffffu, h, o), bl = __shfl_down_sync(0xffffffffu, l, o);
+            float s, e;
+            two_sum(h, bh, s, e);
+            e += l + bl;
+            h = s + e;
+            l = e - (h - s);
+        }
+        if (lane == 0) red[warp * 3 + c] = (double)h + (double)l;
+    }
+    finish_step_red<float>(P, step, b, local, nb_per, red, flag);
 }
 
 template <typename T, int SCHEME, bool VEL, bool PREC>

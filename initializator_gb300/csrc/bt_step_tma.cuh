@@ -498,10 +498,9 @@ __global__ void __launch_bounds__(tma::NT, 2)
 
     // ---- deterministic M(t) reduction (as step_kernel) ----
     {
-        double s3[3] = {acc[0].get(), acc[1].get(), acc[2].get()};
         const unsigned local = (unsigned)zc + (unsigned)P.zsplit * (blockIdx.y + gridDim.y * blockIdx.z);
         const unsigned nb_per = (unsigned)P.zsplit * gridDim.y * gridDim.z;
-        finish_step<float>(P, step, b, local, nb_per, s3, red, const_cast<int*>(&s_flags[1]));
+        finish_step_acc(P, step, b, local, nb_per, acc, red, const_cast<int*>(&s_flags[1]));
     }
     return;
 

@@ -219,7 +219,7 @@ std::string NmrRelaxationSolve::describe() const {
     return s.str();
 }
 
-bt_config NmrRelaxationSolve::make_config() const {
+bt_config NmrRelaxationSolve::make_config(bool gpu_path) const {
     const nmr::Data& d = data_;
     bt_config c{};
     c.nx = nx_;
@@ -227,7 +227,11 @@ bt_config NmrRelaxationSolve::make_config() const {
     c.nz = nz_;
     const char* p = std::getenv("BT_PRECISION");
     c.precision = (p && std::string(p) == "f32") ? BT_F32 : BT_F64;
-    c.scheme = BT_SCHEME_REFERENCE;
+    // solve() steps as the reference's CPU path (ExplicitSimple), solve_gpu() as
+    // its GPU path (the MacCormack ExplicitMakUpgrade); BT_SCHEME=explicit
+    // runs solve_gpu() with ExplicitSimple
+    const char* sch = std::getenv("BT_SCHEME");
+    c.scheme = (gpu_path && !(sch && std::string(sch) == "explicit")) ? BT_SCHEME_MACCORMACK : BT_SCHEME_REFERENCE;
     c.vector_mult = d.nVectorMult;
     c.velocity = d.nVelocity;
     c.diffusion = d.nDiffusion;
@@ -288,7 +292,7 @@ void NmrRelaxationSolve::run(bool gpu_path) {
             if (d.nb[b] != 1)
                 std::cout << "NB" << (b + 1) << " = " << d.nb[b]
                           << ": only zero-derivative (copy) boundaries are implemented; using them" << std::endl;
-    const bt_config c = make_config();
+    const bt_config c = make_config(gpu_path);
     check(bt_create(&c, &h_), "bt_create");
     check(bt_upload_geometry(h_, mask_.data(), vx_.empty() ? nullptr : vx_.data(), vy_.empty() ? nullptr : vy_.data(),
                              vz_.empty() ? nullptr : vz_.data()),

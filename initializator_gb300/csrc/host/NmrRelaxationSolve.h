@@ -59,7 +59,7 @@ private:
     bool initialised_ = false;
     bt_handle* h_ = nullptr;
 
-    bt_config make_config() const;
+    bt_config make_config(bool gpu_path) const;
     void initial_field(std::vector<double>& mx, std::vector<double>& my, std::vector<double>& mz) const;
     void run(bool gpu_path);
     void check(int rc, const char* what) const;

@@ -5,8 +5,9 @@ step, step count, equilibrium magnetization, field direction and gradient as
 the reference's own init() (golden fixtures record them): relative 1e-14,
 step count exact.
 GPU: nmr_exe runs the whole time loop; its CSV rows (6 significant digits, as
-the reference prints them) match the oracle run with the same time step and
-the reference's schedule to 5e-6 relative.
+the reference prints them) match the oracle run with the same time step, the
+reference's schedule and the reference's scheme of that path (solve_gpu:
+MacCormack; solve: ExplicitSimple) to 5e-6 relative.
 """
 import os
 import subprocess
@@ -97,8 +98,10 @@ def test_nmr_exe_end_to_end(case, path, tmp_path, btlib, oracle_lib):
     per_voxel = two or int(z["data_n_surf_rel_water"]) == 1 or int(z["data_n_surf_rel_oil"]) == 1
     _, (p1, p2), _ = coeffs(z)
     fields = (z["t1f"], z["t2f"], z["diff"]) if per_voxel else None
+    # solve_gpu steps with the reference's GPU scheme (MacCormack), solve()
+    # with its CPU scheme (ExplicitSimple)
     res = oracle.run(p, z["mask"], st0, nstep + 1, vel=velocity(z), pulses=pl, fields=fields,
-                     phases=(p1, p2) if two else None)
+                     phases=(p1, p2) if two else None, maccormack=(path == "gpu"))
     mt = res[2] if two else res[1]
     s0 = _phase_sums0(z, st0, p1, p2) if two else oracle.sums(p, z["mask"], st0)[0]
     nd = int(z["data_nd_print"])

@@ -77,3 +77,42 @@ def test_oracle_conservation_no_relaxation(oracle_lib):
     s0, _ = oracle.sums(p, mask, st0)
     _, mt = oracle.run(p, mask, st0, 50)
     assert rel_err(mt[-1], s0) < 1e-12
+
+
+def test_oracle_maccormack_relaxation_known_answer(oracle_lib):
+    """MacCormack on bulk relaxation is Heun's method: per step the transverse
+    field is multiplied by 1 - h + h^2/2 (h = dt/T2) and the longitudinal
+    deviation from p_eq by the same with dt/T1."""
+    import oracle
+    shape = (4, 5, 6)
+    dt, t1, t2, peq = 1e-3, 0.05, 0.02, 0.7
+    p = oracle.make_params(shape, dx=1e-6, dt=dt, main_field=(0, 0, 1), t1=t1, t2=t2, p_eq=peq, diffusion=0)
+    mask = np.ones(shape, np.uint8)
+    st0 = np.zeros((3,) + shape)
+    st0[0] = 1.0
+    st, mt = oracle.run(p, mask, st0, 25, maccormack=True)
+    n = np.arange(1, 26)
+    h2, h1 = dt / t2, dt / t1
+    assert np.allclose(mt[:, 0], (1 - h2 + h2 * h2 / 2) ** n * mask.size, rtol=1e-12)
+    assert np.allclose(mt[:, 2], (peq + (0 - peq) * (1 - h1 + h1 * h1 / 2) ** n) * mask.size, rtol=1e-12)
+
+
+def test_oracle_maccormack_transports_linear_profile(oracle_lib):
+    """Uniform velocity along x, a field linear in x, no relaxation or
+    diffusion: predictor and corrector differences are exact for a linear
+    profile, so away from the domain faces one step moves it by u*dt."""
+    import oracle
+    shape = (3, 3, 16)
+    dx, dt, u = 1e-6, 1e-4, 2e-3
+    p = oracle.make_params(shape, dx=dx, dt=dt, main_field=(0, 0, 1), t1=1e30, t2=1e30, p_eq=0.0, diffusion=0,
+                           velocity=1)
+    mask = np.ones(shape, np.uint8)
+    vx = np.full((3, 3, 17), u)
+    vy = np.zeros((3, 4, 16))
+    vz = np.zeros((4, 3, 16))
+    x = np.arange(16.0)
+    st0 = np.zeros((3,) + shape)
+    st0[1] = 0.5 + 0.01 * x
+    st, _ = oracle.run(p, mask, st0, 1, vel=(vx, vy, vz), maccormack=True)
+    expect = 0.5 + 0.01 * x - u * dt / dx * 0.01
+    assert np.allclose(st[1][:, :, 2:-2], expect[2:-2], rtol=0, atol=1e-15)

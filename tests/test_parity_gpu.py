@@ -400,3 +400,64 @@ def test_per_voxel_fields_reset_and_tma_skip(btlib):
             s.set_state(initial_state(z))
             s.set_step(0)
             assert np.array_equal(s.run(20), ref)
+
+
+@pytest.mark.parametrize("shape", [(9, 7, 13), (16, 12, 40), (5, 33, 70)])
+def test_maccormack_matches_oracle(shape, btlib, oracle_lib):
+    """The reference's GPU scheme (predictor-corrector, two launches per
+    step) against the oracle's restatement, with flow and the cross product:
+    FP64 per voxel bit-identical without pulses; with pulses of flags 1 and 2
+    (CUDA's and the C library's cos/sin may differ in the last bit) fields and
+    M(t) within 1e-12; FP32 M(t) within 1e-4."""
+    import initializator_gb300 as bt
+    import oracle
+    mask, vel, st0, kw = _random_case(shape, seed=sum(shape) + 5)
+    n = 40
+    p = oracle.make_params(shape, **kw)
+    for pl in ([], [(5, 2, 0.7, (0.0, 0.6, 0.8)), (13, 1, 2e-3, (0.2, -0.4, 0.9)), (33, 2, math.pi, (1.0, 0.0, 0.0))]):
+        ref, ref_mt = oracle.run(p, mask, st0, n, vel=vel, pulses=pl, maccormack=True)
+        for prec in (bt.BT_F64, bt.BT_F32):
+            with bt.Solver(bt.make_config(shape, precision=prec, scheme=bt.BT_SCHEME_MACCORMACK, **kw)) as s:
+                s.upload_geometry(mask, vel)
+                s.set_state(st0)
+                s.set_schedule(pl)
+                mt = s.run(n)
+                st = s.get_state()
+                assert s.launches >= 2 * n
+            if prec == bt.BT_F64:
+                if not pl:
+                    assert np.array_equal(st, ref), f"max abs diff {np.abs(st - ref).max()}"
+                assert rel_err(st, ref) <= F64_TOL
+                assert rel_err(mt, ref_mt) <= F64_TOL
+            else:
+                assert rel_err(mt, ref_mt) <= F32_MT_TOL
+
+
+@pytest.mark.parametrize("case", ["surfrel", "two_phase"])
+def test_maccormack_per_voxel_fields(case, btlib, oracle_lib):
+    """MacCormack with the reference's per-voxel coefficient arrays (and the
+    two-component sums) against the oracle: FP64 bit-identical."""
+    import initializator_gb300 as bt
+    import oracle
+    from test_fluid_golden import coeffs
+    z = load(case)
+    two = int(z["data_n_components"]) == 2
+    _, (p1, p2), _ = coeffs(z)
+    n = int(z["nsteps"])
+    p = oracle.make_params(z["mask"].shape, **common(z))
+    res = oracle.run(p, z["mask"], initial_state(z), n, vel=velocity(z), pulses=pulses(z),
+                     fields=(z["t1f"], z["t2f"], z["diff"]), phases=(p1, p2) if two else None, maccormack=True)
+    with _solver(z, bt.BT_F64, scheme=bt.BT_SCHEME_MACCORMACK) as s:
+        s.upload_rates(z["t1f"], z["t2f"], z["diff"])
+        if two:
+            s.set_phase_weights(p1, p2)
+        s.set_state(initial_state(z))
+        s.set_schedule(pulses(z))
+        mt = s.run(n)
+        st = s.get_state()
+        mt6 = s.read_mt_phases(n) if two else None
+    assert np.array_equal(st, res[0]), f"max abs diff {np.abs(st - res[0]).max()}"
+    if two:
+        assert rel_err(mt6, res[2]) <= F64_TOL
+    else:
+        assert rel_err(mt, res[1]) <= F64_TOL
