@@ -53,6 +53,23 @@ def rank_info():
     return r, w, lr
 
 
+def max_over_ranks(x: float, device="cuda") -> float:
+    """The largest x over all ranks (a replica job takes as long as its
+    slowest rank); x itself without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job throughput of N replicas: all ranks' units over the slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 def build_workload(device="cpu", seed=SEED):
     from initializator_gb300 import geometry
     mask = geometry.sphere_pack(SHAPE, 10.0, 0.4, seed=seed, device=device)
@@ -382,12 +399,8 @@ def run_ours(args):
     mt = s.read_mt(S)
     if not np.all(np.isfinite(mt)):
         raise RuntimeError("non-finite M(t)")
-    if w > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = nvox * S * args.steps * w / (ms / 1e3)
+    ms = max_over_ranks(ms)
+    value = job_value(nvox * S * args.steps, w, ms / 1e3)
     per_launch_s = ms / 1e3 / (args.steps * S)
     achieved = BYTES_PER_VOXEL_STEP * nvox / per_launch_s / 1e9
     peak, peak_kind = hbm_peak()
@@ -410,12 +423,8 @@ def run_ours(args):
         s.run(S)                 # S time steps, D2H of the S M(t) samples
     barrier()
     e2e_s = time.perf_counter() - t0
-    if w > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = nvox * S * args.steps * w / e2e_s
+    e2e_s = max_over_ranks(e2e_s)
+    e2e = job_value(nvox * S * args.steps, w, e2e_s)
     s.close()
     qsweep = None if args.no_qsweep else run_qsweep(args, lr)
     ragged = None if args.no_ragged else run_ragged(args, lr)
