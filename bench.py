@@ -202,6 +202,61 @@ def run_ragged(args, lr):
                          "frac": v_many * 25 / 1e9 / peak, "peak_kind": peak_kind, "bytes_per_voxel_step": 25}}
 
 
+C5_SHAPE = (768, 1024, 1024)  # C5: 1024 x 1024 x 768
+C5_STEPS = 500
+
+
+def run_c5(args, lr):
+    """C5, the largest single-GPU workload: 1024x1024x768 thresholded GRF
+    (sigma 5, porosity 0.2), curl-noise flow up to 2 mm/s, PGSE along z with
+    G = 0.2 T/m, KSPACE FP32: ~805 M voxels, ~30 GB resident. 500 time steps
+    timed after 64 warm-up steps (one launch per step)."""
+    import torch
+
+    import initializator_gb300 as bt
+    from initializator_gb300 import geometry
+    dev = torch.device("cuda", lr)
+    t0 = time.perf_counter()
+    mask = geometry.gaussian_random_field(C5_SHAPE, 5.0, 0.2, seed=SEED + 21, device=dev)
+    vel = geometry.curl_velocity(mask, 5.0, 2.0e-3, seed=SEED + 22, device=dev)
+    gen_s = time.perf_counter() - t0
+    dt = geometry.stable_dt(1e-6, 2.3e-9)
+    total = 64 + C5_STEPS + 32
+    wave = bt.kspace_waveform_pgse(total, dt, 0.2, 2e-3, 20e-3, axis=(0.0, 0.0, 1.0))
+    kw = dict(dx=1e-6, dt=dt, d_pore=2.3e-9, t1=2.5, t2=2.0, rho1=1e-5, rho2=1e-5, p_eq=1.0, velocity=1,
+              diffusion=1, gamma=bt.GAMMA_PROTON)
+    s = bt.Solver(bt.make_config(C5_SHAPE, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, **kw))
+    s.upload_geometry(mask, vel)
+    del vel
+    s.set_schedule([], grad_wave=wave)
+    mx = torch.as_tensor(mask, device=dev).float().contiguous()
+    zero = torch.zeros_like(mx)
+    s.set_state_device([mx, zero, zero.clone()])
+    del mx, zero
+    zsplit = s.autotune(16)
+    s.run(64)
+    stream = torch.cuda.ExternalStream(s.stream_ptr)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    s.run_async(C5_STEPS)
+    ev1.record(stream)
+    s.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    mt = s.read_mt(C5_STEPS)
+    s.close()
+    nvox = int(np.prod(C5_SHAPE))
+    per = ms / 1e3 / C5_STEPS
+    peak, peak_kind = hbm_peak()
+    return {"workload": "C5: 1024x1024x768 GRF sigma=5 porosity 0.2, curl-noise flow 2 mm/s, PGSE z G=0.2 T/m, FP32",
+            "voxels": nvox, "steps": C5_STEPS, "value": nvox / per, "unit": UNIT, "ms_per_time_step": per * 1e3,
+            "tma_zsplit": zsplit, "finite": bool(np.all(np.isfinite(mt))), "generate_s": gen_s,
+            "roofline": {"bound": "hbm", "achieved": BYTES_PER_VOXEL_STEP * nvox / per / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": BYTES_PER_VOXEL_STEP * nvox / per / 1e9 / peak,
+                         "peak_kind": peak_kind, "bytes_per_voxel_step": BYTES_PER_VOXEL_STEP}}
+
+
 def physics(total_steps):
     import initializator_gb300 as bt
     from initializator_gb300 import geometry
@@ -428,6 +483,7 @@ def run_ours(args):
     s.close()
     qsweep = None if args.no_qsweep else run_qsweep(args, lr)
     ragged = None if args.no_ragged else run_ragged(args, lr)
+    c5 = run_c5(args, lr) if args.c5 else None
 
     out = None
     if r == 0:
@@ -450,6 +506,7 @@ def run_ours(args):
             "clocks": clk,
             "qsweep": qsweep,
             "ragged": ragged,
+            "c5": c5,
         }
         print(json.dumps(out))
     if w > 1:
@@ -467,6 +524,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-qsweep", action="store_true", help="skip the batched 32-gradient q-sweep (C3a) leg")
     ap.add_argument("--no-ragged", action="store_true", help="skip the 48-sample ragged batch (C3b) leg")
+    ap.add_argument("--c5", action="store_true", help="add the 1024x1024x768 (C5, ~30 GB) leg")
     ap.add_argument("--zsplit", type=int, default=0, help="fixed z-chunking of the fast path (skips the autotuner)")
     ap.add_argument("--profile", action="store_true",
                     help="device-resident phase only (for ncu captures); prints no bench line")

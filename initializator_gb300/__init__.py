@@ -252,9 +252,15 @@ class Solver:
         self._check(self._l.bt_set_state(self._h, _dp(st[0]), _dp(st[1]), _dp(st[2])), "set_state")
 
     def set_state_device(self, tensors):
-        """tensors: three contiguous CUDA tensors of the handle's precision."""
+        """tensors: three contiguous CUDA tensors of the handle's precision.
+        The copy waits for the work torch has queued on its current stream and
+        is complete on return, so the tensors may be reused or freed."""
+        import torch
+        hs = self.torch_stream()
+        hs.wait_stream(torch.cuda.current_stream())
         self._check(self._l.bt_set_state_device(self._h, *(ctypes.c_void_p(t.data_ptr()) for t in tensors)),
                     "set_state_device")
+        hs.synchronize()
 
     def get_state(self):
         comps = [np.zeros((self.batch,) + self.shape) for _ in range(3)]
