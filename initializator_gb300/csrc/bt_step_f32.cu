@@ -1,5 +1,7 @@
 // float instantiation of the fused step kernel and its helpers.
 // Compiled with the default -fmad=true (FP32 production path).
+#include <cstdlib>
+
 #include "bt_step_tma.cuh"
 #include "bt_step_mac.cuh"
 
@@ -50,8 +52,20 @@ static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, di
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    step_tma_kernel<SCHEME, VEL, PREC><<<grid, tma::NT, tma::SMEM, s>>>(p, m);
-    return cudaGetLastError();
+    // programmatic dependent launch: the kernel overlaps its step-independent
+    // prologue with the previous launch's tail (BT_NO_PDL turns it off)
+    static const bool pdl = std::getenv("BT_NO_PDL") == nullptr;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(tma::NT);
+    cfg.dynamicSmemBytes = tma::SMEM;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC>, p, m);
 }
 
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,

@@ -151,8 +151,6 @@ __global__ void __launch_bounds__(tma::NT, 2)
     const int z0 = zc * P.zchunk;
     const int z1 = min(nz, z0 + P.zchunk);
     const int d = (zc & 1) ? -1 : 1;
-    const long long step = __ldcg(&P.ctl->step);
-    const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched) * nb + b;
     const int xb = x0 + QX * lane;  // first of this thread's 4 voxels
     const int y = y0 + w;
 
@@ -185,13 +183,11 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
         fence_mbar_init();
         s_flags[0] = 0;
-        for (int q = 0; q < NSTAGE && q < nplanes; ++q) {
-            issue(q, plane_of(q));
-            n_issued++;
-        }
     }
     // per-CTA table indexed by the voxel code (bit 6 pore, bits 0-5 solid
-    // faces): six face diffusion weights, dt/T1, dt/T2; all zero for solid
+    // faces): six face diffusion weights, dt/T1, dt/T2; all zero for solid.
+    // It depends on the launch's parameters only, so with programmatic
+    // dependent launch it is built while the previous step still runs.
     if (tid < 128) {
         const int f = tid & 63;
         const bool pore = tid & 64;
@@ -203,6 +199,18 @@ __global__ void __launch_bounds__(tma::NT, 2)
         s_tab[3 * tid + 1] = make_float4(dm * ((f & 16) ? sz : kz), dm * ((f & 32) ? sz : kz),
                                          pore ? P.dtt1[f] : 0.f, pore ? P.dtt2[f] : 0.f);
     }
+    // everything below reads what the previous step wrote (the field, the
+    // step counter): wait until that grid has completed and its writes are
+    // visible (returns at once when this launch has no programmatic
+    // dependency)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const long long step = __ldcg(&P.ctl->step);
+    const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched) * nb + b;
+    if (tid == 0)
+        for (int q = 0; q < NSTAGE && q < nplanes; ++q) {
+            issue(q, plane_of(q));
+            n_issued++;
+        }
     // lab-frame phases (KSPACE), FP64-reduced arguments, each computed once
     // per CTA: the tile's 128 columns by threads 0..127, its 8 rows by threads
     // 128..135, the chunk's planes by the threads from 136 on (wrapping)
@@ -491,6 +499,9 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
     }
 
+    // this CTA has read all its input: the next step's grid may start its
+    // CTAs (they build their tables, then wait for this grid to complete)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     // the flag is only written inside the march: after this barrier every
     // thread sees its final value, so the branch below is CTA-uniform
     __syncthreads();
