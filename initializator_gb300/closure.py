@@ -378,12 +378,60 @@ def _head(y, m, sg, sh):
     return torch.stack([gr * m[..., 0] - gi * m[..., 1], gr * m[..., 1] + gi * m[..., 0], gz * m[..., 2] + hz], -1)
 
 
-class Closure:
-    """The trained net and the scales of its head; `apply` adds the
-    correction to a coarse handle's field on coarse pore voxels."""
+def _global_gain(y, pore, sg):
+    """Net output (B, ..., 16) -> one complex gain per sample: sg times the
+    mean over pore voxels of channels 0 + i 1."""
+    p = pore[..., 0] if pore.dim() == y.dim() else pore
+    dims = tuple(range(1, y.dim() - 1))
+    n = p.sum(dim=dims).clamp(min=1.0)
+    gr = (y[..., 0] * p).sum(dim=dims) / n * sg
+    gi = (y[..., 1] * p).sum(dim=dims) / n * sg
+    return gr, gi
 
-    def __init__(self, net: Net, sg=1.0, sh=1.0):
-        self.net, self.sg, self.sh = net, float(sg), float(sh)
+
+def make_rollout_pairs(cc: CoarseCase):
+    """Trajectory targets for the global head: along a plain coarse rollout,
+    the field after each step n (what the net sees in a rollout) and the
+    lab-frame sums M (after the step) and R = (fine increment of M(t) over the
+    step) - (coarse increment): the per-step rate error of the rollout itself.
+    A one-step target from a restricted fine state instead carries that
+    state's projection residual, which a self-consistent rollout pays once,
+    not every step."""
+    import torch
+    case = cc.case
+    mf = case.reference_mt(cc.n, precision=0)  # fine M(t) after fine steps 4, 8, ...
+    crs = cc.solver()
+    crs.set_state(cc.initial())
+    prev_c = cc.mt(crs, 0)
+    prev_f = prev_c.copy()  # the restriction keeps the lab-frame sums
+    # steps at and next to an RF pulse: both increments are large and their
+    # difference is dominated by where within the step the pulse acts; they
+    # are left out of the targets
+    near_pulse = {p[0] + o for p in cc.pulses for o in (-1, 0, 1)}
+    pairs = []
+    for n in range(cc.n):
+        crs.run(1)
+        mc = cc.mt(crs, n + 1)
+        r = (mf[n] - prev_f) - (mc - prev_c)
+        if n not in near_pulse:
+            pred = torch.stack([v.clone() for v in crs.field_views()], dim=-1)
+            pairs.append((pred, None, n, (mc[0], mc[1], r[0], r[1])))
+        prev_c, prev_f = mc, mf[n]
+    torch.cuda.synchronize()
+    crs.close()
+    return pairs
+
+
+class Closure:
+    """The trained net and the scales of its head. head "voxel": `apply` adds
+    a per-voxel correction (complex gain on M_xy, gain and offset on M_z) on
+    coarse pore voxels. head "global": the net's gain channels are averaged
+    over the pore voxels into one complex gain per step that multiplies the
+    whole transverse field (a correction of the step's decay and phase rate,
+    with no per-voxel structure)."""
+
+    def __init__(self, net: Net, sg=1.0, sh=1.0, head="voxel"):
+        self.net, self.sg, self.sh, self.head = net, float(sg), float(sh), head
         self._lay = None
 
     def apply(self, solver, cc: CoarseCase, n):
@@ -395,13 +443,74 @@ class Closure:
             m = torch.stack([v.float() for v in views], dim=-1)
             x = self._lay.pack(cc.features(views, n)[None], self.net.device)
             y = self._lay.unpack(self.net.forward(self._lay, x), fp32_rows=True)[0]
+            if self.head == "global":
+                gr, gi = _global_gain(y[None], cc.pore[None], self.sg)
+                mr, mi = m[..., 0].clone(), m[..., 1].clone()
+                views[0].add_(gr[0] * mr - gi[0] * mi)
+                views[1].add_(gr[0] * mi + gi[0] * mr)
+                return
             dm = _head(y, m, self.sg, self.sh) * cc.pore[..., None]
             for c in range(3):
                 views[c].add_(dm[..., c])
 
 
+def _pair_sums(cc: CoarseCase, pair):
+    """Lab-frame transverse sums of a pair: M of the predicted field and R of
+    the residual target (a global gain g closes the step when g M = R)."""
+    from . import coarse as cg
+    pred, res, n = pair
+    k = cg.kvec(cc.wave, cc.kw["gamma"], cc.kw["dt"], n + 1)
+    d = (cc.kw["dx"],) * 3
+    w = cc.phi if cc.pore_average else None
+    R = cg.lab_sums([res[..., c] for c in range(3)], k, d, w)
+    M = cg.lab_sums([pred[..., c] for c in range(3)], k, d, w)
+    return M[0], M[1], R[0], R[1]
+
+
+def _train_global(samples, allp, iters, batch, lr, lr_end, rng, net, log_every):
+    """Training of the global head (see train)."""
+    import math
+
+    import torch
+    shape = samples[0][0].shape
+    lay = PaddedRows(batch, *shape)
+    dy = torch.zeros((lay.rows, CH), dtype=torch.float32, device=net.device)
+    dyv = dy.view(batch, shape[0] + 2, shape[1] + 2, shape[2] + 2, CH)
+    losses = []
+    sh = 1.0
+    # per pair the lab-frame sums M (prediction) and R (residual); the loss
+    # |g M - R|^2 stays well conditioned where the signal is dephased
+    # (M near 0), unlike a fit of g to R / M
+    mr = torch.tensor([p[3] if len(p) > 3 else _pair_sums(cc, p) for cc, p in allp], dtype=torch.float64,
+                      device=net.device)
+    rms_m = float(mr[:, :2].pow(2).sum(dim=1).mean().sqrt()) or 1.0
+    rms_r = float(mr[:, 2:].pow(2).sum(dim=1).mean().sqrt()) or 1.0
+    sgg = rms_r / rms_m
+    mr = (mr / torch.tensor([rms_m, rms_m, rms_r, rms_r], dtype=torch.float64, device=net.device)).float()
+    for it in range(iters):
+        idx = rng.integers(0, len(allp), size=batch)
+        x = torch.stack([allp[i][0].features([allp[i][1][0][..., c] for c in range(3)], allp[i][1][2])
+                         for i in idx])
+        pore = torch.stack([allp[i][0].pore for i in idx])
+        y = lay.unpack(net.forward(lay, lay.pack(x, net.device)), fp32_rows=True).detach().requires_grad_(True)
+        gr, gi = _global_gain(y, pore, 1.0)  # g / sgg
+        t = mr[torch.as_tensor(idx, device=net.device)]
+        er = gr * t[:, 0] - gi * t[:, 1] - t[:, 2]
+        ei = gr * t[:, 1] + gi * t[:, 0] - t[:, 3]
+        loss = (er ** 2 + ei ** 2).mean()
+        loss.backward()
+        losses.append(float(loss.detach()))
+        if log_every and it % log_every == 0:
+            print(f"closure train {it}: loss {float(loss.detach()):.4e}", flush=True)
+        dyv[:, 1:-1, 1:-1, 1:-1, :] = y.grad
+        net.backward(lay, dy)
+        net.adamw(lr=lr_end + 0.5 * (lr - lr_end) * (1 + math.cos(math.pi * it / max(1, iters))))
+    net.check_status()
+    return Closure(net, sgg, sh, head="global"), losses
+
+
 def train(samples, iters, batch=8, lr=2e-3, lr_end=1e-4, seed=0, net=None, vox_weight=1.0, sum_weight=0.1,
-          log_every=0):
+          log_every=0, head="voxel"):
     """AdamW on the closure net over the pairs of several coarse cases
     (samples: list of (CoarseCase, pairs)). Loss, in units of the targets'
     RMS sigma: vox_weight x the mean squared correction error over pore
@@ -413,6 +522,8 @@ def train(samples, iters, batch=8, lr=2e-3, lr_end=1e-4, seed=0, net=None, vox_w
     import torch
     rng = np.random.default_rng(seed)
     allp = [(cc, p) for cc, ps in samples for p in ps]
+    if head == "global":
+        return _train_global(samples, allp, iters, batch, lr, lr_end, rng, net or Net(seed=seed), log_every)
     res2 = torch.stack([(r[..., :2] ** 2).sum() for _, (_, r, _) in allp]).sum()
     m2 = torch.stack([(p[..., :2] ** 2).sum() for _, (p, _, _) in allp]).sum()
     npore = sum(float(cc.pore.sum()) for cc, _ in allp)
@@ -497,7 +608,7 @@ def mt_error(mt, ref):
 
 
 def evaluate(shape=(64, 64, 64), n_coarse=88, n_train=8, iters=1500, g_test=0.2, seed=5, vox_weight=1.0,
-             sum_weight=0.1, pore_average=False, log=print):
+             sum_weight=0.1, pore_average=False, head="voxel", targets="step", log=print):
     """The closure experiment: training pairs from n_train seeded fine PGSE
     cases (alternating sphere packs and Gaussian random fields, G uniform in
     0..0.3 T/m), training, then on two held-out cases (sphere, GRF) the M(t)
@@ -515,13 +626,14 @@ def evaluate(shape=(64, 64, 64), n_coarse=88, n_train=8, iters=1500, g_test=0.2,
         case = Case.pgse(shape, seed=100 + 7 * i, kind=kind, g_amp=float(rng.uniform(0, 0.3)), n_coarse=n_coarse,
                          device="cuda")
         cc = CoarseCase(case, n_coarse, pore_average=pore_average)
-        samples.append((cc, make_pairs(cc)))
+        samples.append((cc, make_rollout_pairs(cc) if targets == "rollout" else make_pairs(cc)))
     t_pairs = time.time() - t0
     t0 = time.time()
-    clo, losses = train(samples, iters, vox_weight=vox_weight, sum_weight=sum_weight)
+    clo, losses = train(samples, iters, vox_weight=vox_weight, sum_weight=sum_weight, head=head,
+                        lr=5e-4 if head == "global" else 2e-3)
     torch.cuda.synchronize()
     t_train = time.time() - t0
-    out = {"shape": list(shape), "coarse_steps": n_coarse, "train_cases": n_train, "iters": iters,
+    out = {"shape": list(shape), "coarse_steps": n_coarse, "train_cases": n_train, "iters": iters, "head": head, "targets": targets,
            "pairs_s": t_pairs, "train_s": t_train, "loss_first": losses[0],
            "loss_last": float(np.mean(losses[-50:])), "held_out": []}
     for kind, s in (("sphere", 900), ("grf", 901)):
@@ -556,6 +668,10 @@ if __name__ == "__main__":
     ap.add_argument("--train-cases", type=int, default=8)
     ap.add_argument("--iters", type=int, default=1500)
     ap.add_argument("--pore-average", action="store_true")
+    ap.add_argument("--head", default="voxel", choices=["voxel", "global"])
+    ap.add_argument("--targets", default="step", choices=["step", "rollout"],
+                    help="one-step targets from restricted fine states, or trajectory targets (global head)")
     a = ap.parse_args()
-    res = evaluate((a.edge,) * 3, a.coarse_steps, a.train_cases, a.iters, pore_average=a.pore_average)
+    res = evaluate((a.edge,) * 3, a.coarse_steps, a.train_cases, a.iters, pore_average=a.pore_average,
+                   head=a.head, targets=a.targets)
     print(json.dumps(res))
