@@ -329,8 +329,10 @@ cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
         }
     } else if (c.precision == BT_F64)
         e = bt::launch_step<double>(h->pd[side], c.scheme, vel, prec, h->grid, h->stream);
-    else if (h->use_tma && !h->fields_d && !step_has_pulse(h, abs_step))
+    else if (h->use_tma && !h->fields_d && !step_has_pulse(h, abs_step)) {
+        h->launches++;  // the fast path's step and its M(t) finish kernel
         e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, h->stream);
+    }
     else
         e = bt::launch_step<float>(h->pf[side], c.scheme, vel, prec, h->grid, h->stream);
     if (e != cudaSuccess || !h->weights_d) return e;
@@ -805,7 +807,9 @@ int run_advance(bt_handle* h, long long* s, long long end, long long limit) {
             CK(h, cudaGraphLaunch(g, h->stream));
             // kernels per step: the step (two for MacCormack) and, with
             // two-component sums, their two reduction kernels
-            const int per_step = (h->cfg.scheme == BT_SCHEME_MACCORMACK ? 2 : 1) + (h->weights_d ? 2 : 0);
+            const bool fast = h->cfg.precision == BT_F32 && h->use_tma && !h->fields_d &&
+                              h->cfg.scheme != BT_SCHEME_MACCORMACK;
+            const int per_step = (h->cfg.scheme == BT_SCHEME_MACCORMACK ? 2 : 1) + (h->weights_d ? 2 : 0) + (fast ? 1 : 0);
             h->launches += (long long)GRAPH_STEPS * per_step;
             *s += GRAPH_STEPS;
         } else {

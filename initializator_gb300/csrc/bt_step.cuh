@@ -126,6 +126,9 @@ __device__ __forceinline__ void lab_phase(double k, int c, double d, T& re, T& i
 // the result does not depend on scheduling), writes M(t), checks it for
 // NaN/Inf and advances the device step counter. red: >= 3 doubles per warp;
 // flag: one shared int.
+template <typename T>
+__device__ __forceinline__ void reduce_partials(const StepParams<T>& P, long long step, unsigned nb_per, double* red);
+
 // the part after each warp's lane 0 has written its 3 sums to red
 template <typename T>
 __device__ __forceinline__ void finish_step_red(const StepParams<T>& P, long long step, unsigned b, unsigned local,
@@ -149,6 +152,14 @@ __device__ __forceinline__ void finish_step_red(const StepParams<T>& P, long lon
     __syncthreads();
     if (!*flag) return;
     __threadfence();
+    reduce_partials<T>(P, step, nb_per, red);
+}
+
+template <typename T>
+__device__ __forceinline__ void reduce_partials(const StepParams<T>& P, long long step, unsigned nb_per, double* red) {
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nthreads / 32;
     const unsigned nb = P.nbatch > 1 ? (unsigned)P.nbatch : 1u;
     const long long slot = step - __ldcg(&P.ctl->mt_base);
     // every thread of the last CTA strides over one member's partials, then a
@@ -233,6 +244,49 @@ __device__ __forceinline__ void finish_step_acc(const StepParams<float>& P, long
         if (lane == 0) red[warp * 3 + c] = (double)h + (double)l;
     }
     finish_step_red<float>(P, step, b, local, nb_per, red, flag);
+}
+
+// FP32 fast path: this CTA's M(t) partial only (float-float per warp, FP64
+// per CTA, plain store); step_finish_kernel, launched after the step, adds
+// the partials and advances the step counter, so no CTA waits on a fence or
+// an atomic ticket
+__device__ __forceinline__ void cta_partial_acc(const StepParams<float>& P, unsigned b, unsigned local, unsigned nb_per,
+                                                const Acc<float> (&acc)[3], double* red) {
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nthreads / 32;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float h = acc[c].s, l = -acc[c].c;  // Acc holds s - c
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float bh = __shfl_down_sync(0xffffffffu, h, o), bl = __shfl_down_sync(0xffffffffu, l, o);
+            float s, e;
+            two_sum(h, bh, s, e);
+            e += l + bl;
+            h = s + e;
+            l = e - (h - s);
+        }
+        if (lane == 0) red[warp * 3 + c] = (double)h + (double)l;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double t[3] = {0.0, 0.0, 0.0};
+        for (int w = 0; w < nwarps; ++w)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) t[c] += red[w * 3 + c];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) P.partials[3ull * ((unsigned long long)b * nb_per + local) + c] = t[c];
+    }
+}
+
+// one CTA: the partials of the step just run (nb_per per batch member) ->
+// M(t), NaN/Inf check, step counter
+template <typename T>
+__global__ void __launch_bounds__(256) step_finish_kernel(const __grid_constant__ StepParams<T> P, unsigned nb_per) {
+    __shared__ double red[(256 / 32) * 3];
+    const long long step = __ldcg(&P.ctl->step);
+    reduce_partials<T>(P, step, nb_per, red);
 }
 
 template <typename T, int SCHEME, bool VEL, bool PREC>

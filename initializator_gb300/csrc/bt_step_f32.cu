@@ -65,7 +65,13 @@ static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, di
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC>, p, m);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC>, p, m);
+    if (e != cudaSuccess) return e;
+    // the step's M(t) and counter from the CTAs' partials
+    const unsigned nb = p.nbatch > 1 ? (unsigned)p.nbatch : 1u;
+    const unsigned nb_per = (grid.x / nb) * grid.y * grid.z;
+    step_finish_kernel<float><<<1, 256, 0, s>>>(p, nb_per);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,

@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
     {
         const unsigned local = (unsigned)zc + (unsigned)P.zsplit * (blockIdx.y + gridDim.y * blockIdx.z);
         const unsigned nb_per = (unsigned)P.zsplit * gridDim.y * gridDim.z;
-        finish_step_acc(P, step, b, local, nb_per, acc, red, const_cast<int*>(&s_flags[1]));
+        cta_partial_acc(P, b, local, nb_per, acc, red);
     }
     return;
 
