@@ -47,6 +47,7 @@ struct bt_handle {
     int cur = 0;
     uint8_t* code = nullptr;
     void* vel[3] = {};
+    float* ucell = nullptr;       // fast path: gated cell velocities [axis][z][y][pitch]
     void* staging = nullptr;      // pinned host buffer, one component in the handle's precision
     bt::StepInfo* steps_d = nullptr;
     long long nsched = 0;
@@ -238,7 +239,7 @@ bool encode(CUtensorMap* m, CUtensorMapDataType t, int rank, void* base, const c
 bool build_maps(bt_handle* h) {
     const bt_config& c = h->cfg;
     const cuuint64_t nx = c.nx, ny = c.ny, nz = c.nz;
-    const cuuint64_t P4 = (cuuint64_t)h->pitch * 4, V4 = (cuuint64_t)h->vxpitch * 4;
+    const cuuint64_t P4 = (cuuint64_t)h->pitch * 4;
     for (int s = 0; s < 2; ++s) {
         bt::TmaMaps& M = h->maps[s];
         std::memset(&M, 0, sizeof(M));
@@ -255,15 +256,11 @@ bool build_maps(bt_handle* h) {
             if (!encode(&M.code, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, h->code, dims, str, box)) return false;
         }
         if (c.velocity == 1) {
-            cuuint64_t dx_[3] = {nx + 1, ny, nz}, sx[2] = {V4, V4 * ny};
-            cuuint32_t bx[3] = {bt::TMA_TX + 4, bt::TMA_TY, 1};
-            if (!encode(&M.vx, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->vel[0], dx_, sx, bx)) return false;
-            cuuint64_t dy_[3] = {nx, ny + 1, nz}, sy[2] = {P4, P4 * (ny + 1)};
-            cuuint32_t by[3] = {bt::TMA_TX, bt::TMA_TY + 1, 1};
-            if (!encode(&M.vy, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->vel[1], dy_, sy, by)) return false;
-            cuuint64_t dz_[3] = {nx, ny, nz + 1}, sz[2] = {P4, P4 * ny};
-            cuuint32_t bz[3] = {bt::TMA_TX, bt::TMA_TY, 1};
-            if (!encode(&M.vz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h->vel[2], dz_, sz, bz)) return false;
+            if (!h->ucell) return false;
+            cuuint64_t dims[4] = {nx, ny, nz, 3};
+            cuuint64_t str[3] = {P4, P4 * ny, (cuuint64_t)h->comp * 4};
+            cuuint32_t box[4] = {bt::TMA_TX, bt::TMA_TY, 1, 3};
+            if (!encode(&M.ucell, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->ucell, dims, str, box)) return false;
         }
     }
     return true;
@@ -594,6 +591,10 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
             if (cudaMalloc(&h->vel[a], h->esz * n3[a]) != cudaSuccess) return bail(BT_E_NOMEM);
             cudaMemset(h->vel[a], 0, h->esz * n3[a]);
         }
+        if (cfg->precision == BT_F32 && cfg->scheme != BT_SCHEME_MACCORMACK && !std::getenv("BT_NO_TMA")) {
+            if (cudaMalloc(&h->ucell, sizeof(float) * 3 * h->comp) != cudaSuccess) return bail(BT_E_NOMEM);
+            cudaMemset(h->ucell, 0, sizeof(float) * 3 * h->comp);
+        }
     }
     if (cfg->precision == BT_F32 && cudaMallocHost(&h->staging, 4 * h->nvox) != cudaSuccess) return bail(BT_E_NOMEM);
     if (cfg->batch < 0 || (long long)h->nb * (long long)h->comp * 3 > (1LL << 40)) return bail(BT_E_ARG);
@@ -625,6 +626,7 @@ int bt_destroy(bt_handle* h) {
         if (p) cudaFree(p);
     for (auto& p : h->vel)
         if (p) cudaFree(p);
+    if (h->ucell) cudaFree(h->ucell);
     if (h->code) cudaFree(h->code);
     if (h->steps_d) cudaFree(h->steps_d);
     if (h->pulses_d) cudaFree(h->pulses_d);
@@ -676,6 +678,10 @@ int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, cons
                 CK(h, cudaMemcpy2D(h->vel[a], p3[a] * 4, f.data(), w3[a] * 4, w3[a] * 4, rows3[a],
                                    cudaMemcpyHostToDevice));
             }
+        }
+        if (h->ucell) {
+            CK(h, bt::launch_cell_velocity(h->pt[0], h->ucell, (long long)h->comp, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
         }
     }
     h->geometry = true;

@@ -96,7 +96,8 @@ struct StepParams {
 // TMA descriptors of the FP32 fast path (one per ping-pong input side)
 struct TmaMaps {
     CUtensorMap state;   // 4D {x, y, z, component} over the input field
-    CUtensorMap vx, vy, vz, code;
+    CUtensorMap ucell;   // 4D {x, y, z, axis} over the upwind cell velocities
+    CUtensorMap code;
 };
 
 // launchers (bt_step_f32.cu / bt_step_f64.cu)
@@ -115,6 +116,8 @@ cudaError_t launch_phase_sums(const StepParams<T>& p, const T* w1, const T* w2, 
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
                             cudaStream_t s);
 int tma_smem_bytes();
+// upwind cell velocities of the fast path from the face velocities, [axis][z][y][pitch]
+cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s);
 constexpr int TMA_TX = 128;  // tile width (voxels along x) of the fast path
 constexpr int TMA_TY = 8;    // tile height (rows along y) of the fast path
 template <typename T>

@@ -281,10 +281,16 @@ __device__ __forceinline__ void cta_partial_acc(const StepParams<float>& P, unsi
 }
 
 // one CTA: the partials of the step just run (nb_per per batch member) ->
-// M(t), NaN/Inf check, step counter
+// M(t), NaN/Inf check, step counter.
+// Launched as a programmatic dependent of the step's grid (or after it in
+// plain stream order): it lets the next step's grid start its CTAs at once
+// (they build their tables, then wait for this grid to complete), then waits
+// until the step's CTAs have completed and their partials are visible.
 template <typename T>
 __global__ void __launch_bounds__(256) step_finish_kernel(const __grid_constant__ StepParams<T> P, unsigned nb_per) {
     __shared__ double red[(256 / 32) * 3];
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const long long step = __ldcg(&P.ctl->step);
     reduce_partials<T>(P, step, nb_per, red);
 }

@@ -43,6 +43,11 @@ cudaError_t launch_frame<float>(float* f[3], const uint8_t* code, int nx, int ny
 
 int tma_smem_bytes() { return tma::SMEM; }
 
+cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s) {
+    cell_velocity_kernel<<<1216, 256, 0, s>>>(p, u, comp);
+    return cudaGetLastError();
+}
+
 template <int SCHEME, bool VEL, bool PREC>
 static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, cudaStream_t s) {
     static bool configured = false;
@@ -67,11 +72,15 @@ static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, di
     cfg.numAttrs = pdl ? 1 : 0;
     cudaError_t e = cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC>, p, m);
     if (e != cudaSuccess) return e;
-    // the step's M(t) and counter from the CTAs' partials
+    // the step's M(t) and counter from the CTAs' partials (a programmatic
+    // dependent too: it starts while the step's last CTAs store their partials)
     const unsigned nb = p.nbatch > 1 ? (unsigned)p.nbatch : 1u;
     const unsigned nb_per = (grid.x / nb) * grid.y * grid.z;
-    step_finish_kernel<float><<<1, 256, 0, s>>>(p, nb_per);
-    return cudaGetLastError();
+    cudaLaunchConfig_t fin = cfg;
+    fin.gridDim = dim3(1);
+    fin.blockDim = dim3(256);
+    fin.dynamicSmemBytes = 0;
+    return cudaLaunchKernelEx(&fin, step_finish_kernel<float>, p, nb_per);
 }
 
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,

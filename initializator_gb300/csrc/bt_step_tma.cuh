@@ -4,7 +4,7 @@
 // for steps without pulses:
 //   * a CTA owns a 128 x 8 column tile and marches through a z-chunk;
 //   * each z-plane of the tile (the three field components with a one-voxel
-//     x/y halo, face velocities, geometry code) is fetched by one thread with
+//     x/y halo, upwind cell velocities, geometry code) is fetched by one thread with
 //     cp.async.bulk.tensor into a 3-slot shared-memory ring, completion
 //     tracked by one "full" mbarrier per slot (expect_tx), so two planes are
 //     in flight while the CTA computes the current one; each warp releases a
@@ -18,7 +18,13 @@
 //     w_f * (M_f - M_0), w_f folding harmonic-mean diffusion and first-order
 //     upwind advection, with w_f = 0 on domain faces (copy ghosts give a zero
 //     difference in the reference, cpp:1664-1754) — FP32 only; the FP64 path
-//     keeps the reference's exact operation order in step_kernel.
+//     keeps the reference's exact operation order in step_kernel;
+//   * the advection enters through one value per voxel and axis,
+//     u = dt/(2 d) (v_lo + v_hi), zeroed where the face it draws from (v_hi
+//     for u < 0, v_lo for u > 0) is closed; cell_velocity_kernel forms it once
+//     per geometry upload with the same FP32 operations the per-face form
+//     uses, so the weights are bit-identical to it and a plane's velocities
+//     are one 3 x 128 x 8 box instead of three face boxes with halos.
 // Out-of-range TMA boxes (halo beyond the domain, plane -1 or nz) are
 // zero-filled and never used as data.
 // Every mbarrier wait is bounded; a wait that gives up raises the CTA's
@@ -39,18 +45,13 @@ constexpr int NT = 32 * TH;         // 256 threads, one warp per row
 constexpr int NSTAGE = 3;
 constexpr int SW = TW + 8;          // state tile width: x0-4 .. x0+TW+3
 constexpr int SH = TH + 2;          // state tile height: y0-1 .. y0+TH
-constexpr int VXW = TW + 4;         // vx faces x0 .. x0+TW+3 (TW+1 used)
 constexpr int OFF_STATE = 0;
 constexpr int SZ_STATE = 3 * SH * SW * 4;                   // 16320
-constexpr int OFF_VX = 16384;
-constexpr int SZ_VX = TH * VXW * 4;                         // 4224
-constexpr int OFF_VY = OFF_VX + SZ_VX;                      // 20608
-constexpr int SZ_VY = (TH + 1) * TW * 4;                    // 4608
-constexpr int OFF_VZ = OFF_VY + SZ_VY;                      // 25216
-constexpr int SZ_VZ = TH * TW * 4;                          // 4096
-constexpr int OFF_CODE = OFF_VZ + SZ_VZ;                    // 29312
+constexpr int OFF_U = 16384;
+constexpr int SZ_U = 3 * TH * TW * 4;                       // 12288: upwind cell velocities, 3 axes
+constexpr int OFF_CODE = OFF_U + SZ_U;                      // 28672
 constexpr int SZ_CODE = TH * TW;                            // 1024
-constexpr int STAGE = OFF_CODE + SZ_CODE;                   // 30336
+constexpr int STAGE = OFF_CODE + SZ_CODE;                   // 29696
 constexpr int OFF_AUX = NSTAGE * STAGE;                     // tables, barriers, reduction
 // aux layout (bytes from OFF_AUX)
 constexpr int TAB_ROW = 12;                  // floats per code-table row: 48 B, so 8 distinct rows hit 8 bank groups
@@ -62,7 +63,7 @@ constexpr int AUX_RED = AUX_FLAGS + 128;     // 8 warps x 3 doubles
 constexpr int AUX_EX = AUX_RED + 256;        // exp(-i k_x x), TW float2
 constexpr int AUX_EZ = AUX_EX + 8 * TW;      // exp(-i k_z z), up to ZCHUNK_MAX float2
 constexpr int SMEM = OFF_AUX + AUX_EZ + 8 * ZCHUNK_MAX + 128;  // + 128 for the base alignment
-static_assert(OFF_VX % 128 == 0 && OFF_VY % 128 == 0 && OFF_VZ % 128 == 0 && OFF_CODE % 128 == 0, "align");
+static_assert(OFF_U % 128 == 0 && OFF_CODE % 128 == 0, "align");
 static_assert(STAGE % 128 == 0, "align");
 constexpr uint32_t WAIT_LIMIT = 1u << 20;  // polls; a healthy copy lands in microseconds
 
@@ -117,6 +118,28 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
 
 }  // namespace tma
 
+// one thread per voxel (grid-stride): the fast path's gated cell velocities
+// u[axis][z][y][pitch]; face arrays as StepParams describes them
+__global__ void cell_velocity_kernel(const StepParams<float> P, float* __restrict__ u, long long comp) {
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const float h2[3] = {0.5f * P.hx, 0.5f * P.hy, 0.5f * P.hz};
+    const long long n = (long long)nx * ny * nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q % nx);
+        const long long r = q / nx;  // z * ny + y
+        const int y = (int)(r % ny), z = (int)(r / ny);
+        const float lo[3] = {P.vx[r * P.vxpitch + x], P.vy[((long long)z * (ny + 1) + y) * P.pitch + x],
+                             P.vz[r * P.pitch + x]};
+        const float hi[3] = {P.vx[r * P.vxpitch + x + 1], P.vy[((long long)z * (ny + 1) + y + 1) * P.pitch + x],
+                             P.vz[(r + ny) * P.pitch + x]};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float v = h2[a] * (lo[a] + hi[a]);
+            u[a * comp + r * P.pitch + x] = (v < 0.f ? hi[a] != 0.f : lo[a] != 0.f) ? v : 0.f;
+        }
+    }
+}
+
 template <int SCHEME, bool VEL, bool PREC>
 __global__ void __launch_bounds__(tma::NT, 2)
     step_tma_kernel(const __grid_constant__ StepParams<float> P, const __grid_constant__ TmaMaps M) {
@@ -155,17 +178,13 @@ __global__ void __launch_bounds__(tma::NT, 2)
     const int y = y0 + w;
 
     uint32_t txbytes = SZ_STATE + SZ_CODE;
-    if constexpr (VEL) txbytes += SZ_VX + SZ_VY + SZ_VZ;
+    if constexpr (VEL) txbytes += SZ_U;
     auto issue = [&](int slot, int plane) {
         uint64_t* bar = &bars[slot];
         unsigned char* base = smem + slot * STAGE;
         mbar_expect_tx(bar, txbytes);
         tma_load_5d(base + OFF_STATE, &M.state, bar, x0 - 4, y0 - 1, plane, 0, (int)b);
-        if constexpr (VEL) {
-            tma_load_3d(base + OFF_VX, &M.vx, bar, x0, y0, plane);
-            tma_load_3d(base + OFF_VY, &M.vy, bar, x0, y0, plane);
-            tma_load_3d(base + OFF_VZ, &M.vz, bar, x0, y0, plane);
-        }
+        if constexpr (VEL) tma_load_4d(base + OFF_U, &M.ucell, bar, x0, y0, plane, 0);
         tma_load_3d(base + OFF_CODE, &M.code, bar, x0, y0, plane);
     };
     // plane sequence: q = 0 is the ghost-side plane, then the chunk in marching order
@@ -246,7 +265,6 @@ __global__ void __launch_bounds__(tma::NT, 2)
             ph[a][1] = (float)si->phase[2 * a][1];
         }
     }
-    const float hx2 = 0.5f * P.hx, hy2 = 0.5f * P.hy, hz2 = 0.5f * P.hz;
     // summation mask of this thread's 4 voxels (trimming box, inside the grid)
     uint32_t xmask = 0;
 #pragma unroll
@@ -260,7 +278,6 @@ __global__ void __launch_bounds__(tma::NT, 2)
 
     Acc<float> acc[3];
     float prv[3][QX], cur[3][QX], nxt[3][QX];
-    float vzc[QX] = {0.f, 0.f, 0.f, 0.f}, vzp[QX] = {0.f, 0.f, 0.f, 0.f}, vzn[QX] = {0.f, 0.f, 0.f, 0.f};
 
     auto own = [&](int slot, float (&dst)[3][QX]) {
         const float* st = reinterpret_cast<const float*>(smem + slot * STAGE + OFF_STATE);
@@ -268,12 +285,6 @@ __global__ void __launch_bounds__(tma::NT, 2)
         for (int c = 0; c < 3; ++c) {
             const float4 v = *reinterpret_cast<const float4*>(st + (c * SH + w + 1) * SW + 4 + QX * lane);
             dst[c][0] = v.x; dst[c][1] = v.y; dst[c][2] = v.z; dst[c][3] = v.w;
-        }
-    };
-    auto own_vz = [&](int slot, float (&dst)[QX]) {
-        if constexpr (VEL) {
-            const float4 v = *reinterpret_cast<const float4*>(smem + slot * STAGE + OFF_VZ + 4 * (w * TW + QX * lane));
-            dst[0] = v.x; dst[1] = v.y; dst[2] = v.z; dst[3] = v.w;
         }
     };
     // s_flags[0] is the CTA's failure flag (volatile: polled inside waits)
@@ -316,12 +327,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
         live = wait_full(0);
         if (live) {
             own(0, prv);
-            own_vz(0, vzp);
             live = wait_full(1);
         }
         if (live) {
             own(1, cur);
-            own_vz(1, vzc);
             release(0);
             if (tid == 0 && nplanes > NSTAGE) refill(NSTAGE);
         }
@@ -333,11 +342,9 @@ __global__ void __launch_bounds__(tma::NT, 2)
         if (!wait_full(q + 1)) break;
         const int sn = (q + 1) % NSTAGE;
         own(sn, nxt);
-        own_vz(sn, vzn);
         // one instance of the plane body per marching direction, so that
-        // below / above and the upper face velocity bind to fixed registers
-        auto body = [&](const float(&bel)[3][QX], const float(&abv)[3][QX], const float(&whi)[QX]) {
-        const float(&wlo)[QX] = vzc;  // face z; whi is face z+1
+        // below / above bind to fixed registers
+        auto body = [&](const float(&bel)[3][QX], const float(&abv)[3][QX]) {
         const unsigned char* base = smem + sc * STAGE;
         const float* st = reinterpret_cast<const float*>(base + OFF_STATE);
         float xm[3][QX], xp[3][QX], ym[3][QX], yp[3][QX];
@@ -362,19 +369,15 @@ __global__ void __launch_bounds__(tma::NT, 2)
             for (int i = 0; i < QX - 1; ++i) xp[c][i] = cur[c][i + 1];
         }
         const uint32_t code4 = *reinterpret_cast<const uint32_t*>(base + OFF_CODE + w * TW + QX * lane);
-        float vxf[QX + 1] = {0.f, 0.f, 0.f, 0.f, 0.f}, vyl[QX] = {0.f, 0.f, 0.f, 0.f}, vyh[QX] = {0.f, 0.f, 0.f, 0.f};
+        float ux[QX] = {0.f, 0.f, 0.f, 0.f}, uy[QX] = {0.f, 0.f, 0.f, 0.f}, uz[QX] = {0.f, 0.f, 0.f, 0.f};
         if constexpr (VEL) {
-            const float* vxr = reinterpret_cast<const float*>(base + OFF_VX) + w * VXW + QX * lane;
-            const float4 a = *reinterpret_cast<const float4*>(vxr);
-            vxf[0] = a.x; vxf[1] = a.y; vxf[2] = a.z; vxf[3] = a.w;
-            float r = __shfl_down_sync(0xffffffffu, a.x, 1);
-            if (lane == 31) r = vxr[QX];
-            vxf[QX] = r;
-            const float* vyr = reinterpret_cast<const float*>(base + OFF_VY) + w * TW + QX * lane;
-            const float4 b = *reinterpret_cast<const float4*>(vyr);
-            const float4 c = *reinterpret_cast<const float4*>(vyr + TW);
-            vyl[0] = b.x; vyl[1] = b.y; vyl[2] = b.z; vyl[3] = b.w;
-            vyh[0] = c.x; vyh[1] = c.y; vyh[2] = c.z; vyh[3] = c.w;
+            const float* ur = reinterpret_cast<const float*>(base + OFF_U) + w * TW + QX * lane;
+            const float4 a = *reinterpret_cast<const float4*>(ur);
+            const float4 b = *reinterpret_cast<const float4*>(ur + TH * TW);
+            const float4 c = *reinterpret_cast<const float4*>(ur + 2 * TH * TW);
+            ux[0] = a.x; ux[1] = a.y; ux[2] = a.z; ux[3] = a.w;
+            uy[0] = b.x; uy[1] = b.y; uy[2] = b.z; uy[3] = b.w;
+            uz[0] = c.x; uz[1] = c.y; uz[2] = c.z; uz[3] = c.w;
         }
         const bool edge = xy_edge || z == 0 || z == nz - 1;
         const uint32_t smask = (row_sum && z >= P.box[4] && z < P.box[5]) ? xmask : 0u;
@@ -387,14 +390,14 @@ __global__ void __launch_bounds__(tma::NT, 2)
             float wxm = ta.x, wxp = ta.y, wym = ta.z, wyp = ta.w, wzm = tb.x, wzp = tb.y;
             const float dtt1 = tb.z, dtt2 = tb.w;
             if constexpr (VEL) {
-                // upwind: +face -h min(u,0) s+, -face +h max(u,0) s-, u the cell average
-                const float ux = hx2 * (vxf[i] + vxf[i + 1]), uy = hy2 * (vyl[i] + vyh[i]), uz = hz2 * (wlo[i] + whi[i]);
-                wxp -= vxf[i + 1] != 0.f ? fminf(ux, 0.f) : 0.f;
-                wxm += vxf[i] != 0.f ? fmaxf(ux, 0.f) : 0.f;
-                wyp -= vyh[i] != 0.f ? fminf(uy, 0.f) : 0.f;
-                wym += vyl[i] != 0.f ? fmaxf(uy, 0.f) : 0.f;
-                wzp -= whi[i] != 0.f ? fminf(uz, 0.f) : 0.f;
-                wzm += wlo[i] != 0.f ? fmaxf(uz, 0.f) : 0.f;
+                // upwind: +face -min(u,0), -face +max(u,0), u the gated cell
+                // average (zero where the face it draws from is closed)
+                wxp -= fminf(ux[i], 0.f);
+                wxm += fmaxf(ux[i], 0.f);
+                wyp -= fminf(uy[i], 0.f);
+                wym += fmaxf(uy[i], 0.f);
+                wzp -= fminf(uz[i], 0.f);
+                wzm += fmaxf(uz[i], 0.f);
             }
             if (edge) {
                 const int x = xb + i;
@@ -481,8 +484,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
                 *reinterpret_cast<float4*>(P.out[c] + off) = make_float4(o[c][0], o[c][1], o[c][2], o[c][3]);
         }
         };
-        if (d > 0) body(prv, nxt, vzn);
-        else body(nxt, prv, vzp);
+        if (d > 0) body(prv, nxt);
+        else body(nxt, prv);
         release(q);
         if (tid == 0 && q + NSTAGE < nplanes) refill(q + NSTAGE);
 #pragma unroll
@@ -492,11 +495,6 @@ __global__ void __launch_bounds__(tma::NT, 2)
                 prv[c][i] = cur[c][i];
                 cur[c][i] = nxt[c][i];
             }
-#pragma unroll
-        for (int i = 0; i < QX; ++i) {
-            vzp[i] = vzc[i];
-            vzc[i] = vzn[i];
-        }
     }
 
     // this CTA has read all its input: the next step's grid may start its
