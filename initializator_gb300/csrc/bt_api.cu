@@ -58,6 +58,11 @@ struct bt_handle {
     bt::Ctl* ctl_h = nullptr;     // pinned
     double* partials_d = nullptr;
     size_t partials_cap = 0;
+    size_t tpart = 0;             // fast path: doubles of partials per input side (two sides back to back)
+    // fast path: the last step enqueued was a fast step whose partials wait
+    // for the next fast step or a finish kernel (on input side fast_side)
+    bool fast_pending = false;
+    int fast_side = 0;
     double* mt_d = nullptr;
     long long mt_cap = 0;
     long long step = 0;
@@ -71,6 +76,7 @@ struct bt_handle {
     bt::StepParams<float> pt[2];  // TMA path (own z-chunking)
     bt::TmaMaps maps[2];
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_launches[2] = {0, 0};  // kernels one replay of each graph launches
     long long launches = 0;
     // per-voxel mode: [8][nz][ny][pitch] in the handle's precision: dTime/T1,
     // dTime/T2, then the face diffusivities -x +x -y +y -z +z
@@ -195,6 +201,8 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
         P.pulses = h->pulses_d;
         P.ctl = h->ctl_d;
         P.partials = h->partials_d;
+        P.partials_prev = h->partials_d;
+        P.side = s;
         P.mt = h->mt_d;
         P.mt_cap = h->mt_cap;
         P.fstride = (long long)h->comp;
@@ -209,6 +217,12 @@ void refresh_params(bt_handle* h) {
     } else {
         fill_params<float>(h, h->pf, h->gzsplit);
         fill_params<float>(h, h->pt, h->tzsplit);
+        // the fast path keeps one partials buffer per input side: a step's
+        // partials are read by the next step, which writes the other buffer
+        for (int s = 0; s < 2; ++s) {
+            h->pt[s].partials = h->partials_d + s * h->tpart;
+            h->pt[s].partials_prev = h->partials_d + (1 - s) * h->tpart;
+        }
     }
     drop_graphs(h);
 }
@@ -280,7 +294,8 @@ int set_tma_split(bt_handle* h, int zsplit) {
     const int gx = (c.nx + bt::TMA_TX - 1) / bt::TMA_TX, gy = (c.ny + bt::TMA_TY - 1) / bt::TMA_TY;
     h->tzsplit = zsplit;
     h->tgrid = dim3(zsplit * h->nb, gx, gy);
-    const size_t need = 3 * (size_t)zsplit * gx * gy * h->nb;
+    h->tpart = 3 * (size_t)zsplit * gx * gy * h->nb;
+    const size_t need = 2 * h->tpart;
     if (need > h->partials_cap) {
         if (h->partials_d) cudaFree(h->partials_d);
         h->partials_d = nullptr;
@@ -308,30 +323,50 @@ bool step_has_pulse(const bt_handle* h, long long s) {
     return s < h->nsched && h->steps_h[s * h->nb].pulse_count > 0;
 }
 
+// close a run of fast steps: the finish kernel adds the last step's partials
+// and brings Ctl::step up to date (a no-op when nothing is pending)
+cudaError_t finish_fast(bt_handle* h) {
+    if (!h->fast_pending) return cudaSuccess;
+    h->fast_pending = false;
+    h->launches++;
+    return bt::launch_tma_finish(h->pt[h->fast_side], h->tgrid, h->stream);
+}
+
 cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
     const bt_config& c = h->cfg;
     const int prec = (c.scheme != BT_SCHEME_KSPACE && c.vector_mult == 1) ? 1 : 0;
     const int vel = c.velocity == 1 ? 1 : 0;
-    h->launches++;
+    const bool fast = c.precision == BT_F32 && c.scheme != BT_SCHEME_MACCORMACK && h->use_tma && !h->fields_d &&
+                      !step_has_pulse(h, abs_step);
     cudaError_t e;
-    if (c.scheme == BT_SCHEME_MACCORMACK) {
-        h->launches++;  // predictor + corrector
-        char* pb = static_cast<char*>(h->pred_base);
-        if (c.precision == BT_F64) {
-            double* pr[3] = {(double*)pb, (double*)(pb + 8 * h->comp), (double*)(pb + 16 * h->comp)};
-            e = bt::launch_mac<double>(h->pd[side], pr, vel, prec, h->grid, h->stream);
-        } else {
-            float* pr[3] = {(float*)pb, (float*)(pb + 4 * h->comp), (float*)(pb + 8 * h->comp)};
-            e = bt::launch_mac<float>(h->pf[side], pr, vel, prec, h->grid, h->stream);
-        }
-    } else if (c.precision == BT_F64)
-        e = bt::launch_step<double>(h->pd[side], c.scheme, vel, prec, h->grid, h->stream);
-    else if (h->use_tma && !h->fields_d && !step_has_pulse(h, abs_step)) {
-        h->launches++;  // the fast path's step and its M(t) finish kernel
-        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, h->stream);
+    if (fast) {
+        // a fast step after a fast step adds its predecessor's partials
+        h->launches++;
+        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, !h->fast_pending,
+                                h->stream);
+        h->fast_pending = true;
+        h->fast_side = side;
+        // the two-component sums read Ctl::step
+        if (e == cudaSuccess && h->weights_d) e = finish_fast(h);
+    } else {
+        e = finish_fast(h);
+        if (e != cudaSuccess) return e;
+        h->launches++;
+        if (c.scheme == BT_SCHEME_MACCORMACK) {
+            h->launches++;  // predictor + corrector
+            char* pb = static_cast<char*>(h->pred_base);
+            if (c.precision == BT_F64) {
+                double* pr[3] = {(double*)pb, (double*)(pb + 8 * h->comp), (double*)(pb + 16 * h->comp)};
+                e = bt::launch_mac<double>(h->pd[side], pr, vel, prec, h->grid, h->stream);
+            } else {
+                float* pr[3] = {(float*)pb, (float*)(pb + 4 * h->comp), (float*)(pb + 8 * h->comp)};
+                e = bt::launch_mac<float>(h->pf[side], pr, vel, prec, h->grid, h->stream);
+            }
+        } else if (c.precision == BT_F64)
+            e = bt::launch_step<double>(h->pd[side], c.scheme, vel, prec, h->grid, h->stream);
+        else
+            e = bt::launch_step<float>(h->pf[side], c.scheme, vel, prec, h->grid, h->stream);
     }
-    else
-        e = bt::launch_step<float>(h->pf[side], c.scheme, vel, prec, h->grid, h->stream);
     if (e != cudaSuccess || !h->weights_d) return e;
     // two-component sums of the field this step wrote
     h->launches += 2;
@@ -782,6 +817,7 @@ int run_begin(bt_handle* h, long long nsteps) {
     h->ctl_h->ticket = 0;
     h->ctl_h->status = 0;
     CK(h, cudaMemcpyAsync(h->ctl_d, h->ctl_h, sizeof(bt::Ctl), cudaMemcpyHostToDevice, h->stream));
+    h->fast_pending = false;  // a run that failed part-way may have left one
     h->last_run = nsteps;
     return BT_OK;
 }
@@ -795,6 +831,8 @@ int run_advance(bt_handle* h, long long* s, long long end, long long limit) {
         bool clean = stop - *s >= GRAPH_STEPS;
         for (long long q = *s; clean && q < *s + GRAPH_STEPS; ++q) clean = !step_has_pulse(h, q);
         if (clean) {
+            // a graph starts and ends with no fast step pending
+            CK(h, finish_fast(h));
             cudaGraphExec_t& g = h->graph[h->cur];
             if (!g) {
                 cudaGraph_t graph;
@@ -802,6 +840,9 @@ int run_advance(bt_handle* h, long long* s, long long end, long long limit) {
                 cudaError_t e = cudaSuccess;
                 const long long before = h->launches;
                 for (int q = 0; q < GRAPH_STEPS && e == cudaSuccess; ++q) e = launch_one(h, (h->cur + q) & 1, *s + q);
+                if (e == cudaSuccess) e = finish_fast(h);
+                h->fast_pending = false;
+                h->graph_launches[h->cur] = h->launches - before;
                 h->launches = before;
                 cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
                 CK(h, e);
@@ -811,12 +852,7 @@ int run_advance(bt_handle* h, long long* s, long long end, long long limit) {
                 CK(h, e);
             }
             CK(h, cudaGraphLaunch(g, h->stream));
-            // kernels per step: the step (two for MacCormack) and, with
-            // two-component sums, their two reduction kernels
-            const bool fast = h->cfg.precision == BT_F32 && h->use_tma && !h->fields_d &&
-                              h->cfg.scheme != BT_SCHEME_MACCORMACK;
-            const int per_step = (h->cfg.scheme == BT_SCHEME_MACCORMACK ? 2 : 1) + (h->weights_d ? 2 : 0) + (fast ? 1 : 0);
-            h->launches += (long long)GRAPH_STEPS * per_step;
+            h->launches += h->graph_launches[h->cur];
             *s += GRAPH_STEPS;
         } else {
             CK(h, launch_one(h, h->cur, *s));
@@ -824,6 +860,7 @@ int run_advance(bt_handle* h, long long* s, long long end, long long limit) {
             *s += 1;
         }
     }
+    CK(h, finish_fast(h));
     h->step = *s;
     return BT_OK;
 }

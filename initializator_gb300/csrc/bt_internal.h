@@ -44,6 +44,11 @@ struct Ctl {
     long long mt_base;   // step whose sums go to mt[0]
     unsigned int ticket; // CTAs of the current launch that have finished
     int status;          // 0 ok, 1 = M(t) buffer overflow, 2 = schedule missing
+    // FP32 fast path, inside a run of consecutive fast steps: the step index
+    // of the next launch on each ping-pong input side (a step on side s reads
+    // fstep[s] and writes fstep[1 - s]; step is brought up to date by the
+    // finish kernel that closes the run)
+    long long fstep[2];
 };
 
 // Device layouts are pitched so that every row starts on a 16-byte boundary
@@ -81,6 +86,8 @@ struct StepParams {
     const DevPulse* pulses;
     Ctl* ctl;
     double* partials;           // [nbatch][CTAs per member][3]
+    const double* partials_prev;  // fast path: the other input side's partials (the previous step's)
+    int side;                   // ping-pong input side these parameters read
     double* mt;                 // [mt_cap][nbatch][3]
     long long mt_cap;           // steps
     // per-voxel mode (SurfRel*.dat face relaxivities, two-component fluids):
@@ -112,9 +119,14 @@ cudaError_t launch_mac(const StepParams<T>& p, T* const pred[3], int vel, int pr
 template <typename T>
 cudaError_t launch_phase_sums(const StepParams<T>& p, const T* w1, const T* w2, double* part6, int nblocks,
                               double* mt6, long long cap, cudaStream_t s);
-// FP32 fast path: TMA-staged plane tiles, 4 voxels per thread, no pulses
+// FP32 fast path: TMA-staged plane tiles, 4 voxels per thread, no pulses.
+// A run of consecutive fast steps: the first launch has first = true (it
+// reads Ctl::step); each later one also reduces its predecessor's partials
+// into M(t); launch_tma_finish(last step's parameters) closes the run (the last
+// step's M(t), Ctl::step)
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
-                            cudaStream_t s);
+                            bool first, cudaStream_t s);
+cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_t s);
 int tma_smem_bytes();
 // upwind cell velocities of the fast path from the face velocities, [axis][z][y][pitch]
 cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s);

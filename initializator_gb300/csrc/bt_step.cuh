@@ -155,20 +155,22 @@ __device__ __forceinline__ void finish_step_red(const StepParams<T>& P, long lon
     reduce_partials<T>(P, step, nb_per, red);
 }
 
+// all threads of one CTA: step's M(t) (one row per batch member) from the
+// per-CTA partials parts, NaN/Inf check; ends with a CTA barrier
 template <typename T>
-__device__ __forceinline__ void reduce_partials(const StepParams<T>& P, long long step, unsigned nb_per, double* red) {
+__device__ __forceinline__ void reduce_members(const StepParams<T>& P, const double* parts, long long step,
+                                               unsigned nb_per, double* red) {
     const int nthreads = blockDim.x * blockDim.y;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int lane = tid & 31, warp = tid >> 5, nwarps = nthreads / 32;
     const unsigned nb = P.nbatch > 1 ? (unsigned)P.nbatch : 1u;
     const long long slot = step - __ldcg(&P.ctl->mt_base);
-    // every thread of the last CTA strides over one member's partials, then a
-    // fixed tree; this tail runs after all other CTAs, on the step's critical path
+    // every thread strides over one member's partials, then a fixed tree
     for (unsigned bb = 0; bb < nb; ++bb) {
         double t[3] = {0.0, 0.0, 0.0};
         for (unsigned q = tid; q < nb_per; q += nthreads)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) t[c] += __ldcg(&P.partials[3ull * ((unsigned long long)bb * nb_per + q) + c]);
+            for (int c = 0; c < 3; ++c) t[c] += __ldcg(&parts[3ull * ((unsigned long long)bb * nb_per + q) + c]);
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -193,7 +195,14 @@ __device__ __forceinline__ void reduce_partials(const StepParams<T>& P, long lon
         }
     }
     __syncthreads();
-    if (tid == 0) {
+}
+
+// the last CTA of a launch (or a finish kernel): M(t) of the step, then the
+// step counter
+template <typename T>
+__device__ __forceinline__ void reduce_partials(const StepParams<T>& P, long long step, unsigned nb_per, double* red) {
+    reduce_members<T>(P, P.partials, step, nb_per, red);
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) {
         P.ctl->ticket = 0;
         P.ctl->step = step + 1;
         __threadfence();
@@ -247,9 +256,8 @@ __device__ __forceinline__ void finish_step_acc(const StepParams<float>& P, long
 }
 
 // FP32 fast path: this CTA's M(t) partial only (float-float per warp, FP64
-// per CTA, plain store); step_finish_kernel, launched after the step, adds
-// the partials and advances the step counter, so no CTA waits on a fence or
-// an atomic ticket
+// per CTA, plain store); the next fast step (or the finish kernel closing the
+// run) adds the partials, so no CTA waits on a fence or an atomic ticket
 __device__ __forceinline__ void cta_partial_acc(const StepParams<float>& P, unsigned b, unsigned local, unsigned nb_per,
                                                 const Acc<float> (&acc)[3], double* red) {
     const int nthreads = blockDim.x * blockDim.y;
@@ -280,18 +288,19 @@ __device__ __forceinline__ void cta_partial_acc(const StepParams<float>& P, unsi
     }
 }
 
-// one CTA: the partials of the step just run (nb_per per batch member) ->
-// M(t), NaN/Inf check, step counter.
+// one CTA, closing a run of fast-path steps: the partials of the run's last
+// step (P: that step's parameters; nb_per per batch member) -> M(t), NaN/Inf
+// check, Ctl::step.
 // Launched as a programmatic dependent of the step's grid (or after it in
-// plain stream order): it lets the next step's grid start its CTAs at once
-// (they build their tables, then wait for this grid to complete), then waits
-// until the step's CTAs have completed and their partials are visible.
+// plain stream order): it lets the next grid start its CTAs at once (they
+// build their tables, then wait for this grid to complete), then waits until
+// the step's CTAs have completed and their partials and counter are visible.
 template <typename T>
 __global__ void __launch_bounds__(256) step_finish_kernel(const __grid_constant__ StepParams<T> P, unsigned nb_per) {
     __shared__ double red[(256 / 32) * 3];
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    const long long step = __ldcg(&P.ctl->step);
+    const long long step = __ldcg(&P.ctl->fstep[1 - P.side]) - 1;
     reduce_partials<T>(P, step, nb_per, red);
 }
 

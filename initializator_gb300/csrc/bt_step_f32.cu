@@ -48,8 +48,24 @@ cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long
     return cudaGetLastError();
 }
 
+// programmatic dependent launch: a kernel overlaps its step-independent
+// prologue with the previous launch's tail (BT_NO_PDL turns it off)
+static cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, int smem, cudaStream_t s, cudaLaunchAttribute* attr) {
+    static const bool pdl = std::getenv("BT_NO_PDL") == nullptr;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cfg;
+}
+
 template <int SCHEME, bool VEL, bool PREC>
-static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, cudaStream_t s) {
+static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, bool first, cudaStream_t s) {
     static bool configured = false;
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC>,
@@ -57,42 +73,29 @@ static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, di
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    // programmatic dependent launch: the kernel overlaps its step-independent
-    // prologue with the previous launch's tail (BT_NO_PDL turns it off)
-    static const bool pdl = std::getenv("BT_NO_PDL") == nullptr;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = dim3(tma::NT);
-    cfg.dynamicSmemBytes = tma::SMEM;
-    cfg.stream = s;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = pdl ? 1 : 0;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC>, p, m);
-    if (e != cudaSuccess) return e;
-    // the step's M(t) and counter from the CTAs' partials (a programmatic
-    // dependent too: it starts while the step's last CTAs store their partials)
+    const cudaLaunchConfig_t cfg = pdl_config(grid, dim3(tma::NT), tma::SMEM, s, attr);
+    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC>, p, m, first ? 1 : 0);
+}
+
+cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_t s) {
     const unsigned nb = p.nbatch > 1 ? (unsigned)p.nbatch : 1u;
     const unsigned nb_per = (grid.x / nb) * grid.y * grid.z;
-    cudaLaunchConfig_t fin = cfg;
-    fin.gridDim = dim3(1);
-    fin.blockDim = dim3(256);
-    fin.dynamicSmemBytes = 0;
-    return cudaLaunchKernelEx(&fin, step_finish_kernel<float>, p, nb_per);
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t cfg = pdl_config(dim3(1), dim3(256), 0, s, attr);
+    return cudaLaunchKernelEx(&cfg, step_finish_kernel<float>, p, nb_per);
 }
 
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
-                            cudaStream_t s) {
+                            bool first, cudaStream_t s) {
     if (scheme == SCHEME_REF) {
-        if (vel && prec) return launch_tma_t<SCHEME_REF, true, true>(p, m, grid, s);
-        if (vel) return launch_tma_t<SCHEME_REF, true, false>(p, m, grid, s);
-        if (prec) return launch_tma_t<SCHEME_REF, false, true>(p, m, grid, s);
-        return launch_tma_t<SCHEME_REF, false, false>(p, m, grid, s);
+        if (vel && prec) return launch_tma_t<SCHEME_REF, true, true>(p, m, grid, first, s);
+        if (vel) return launch_tma_t<SCHEME_REF, true, false>(p, m, grid, first, s);
+        if (prec) return launch_tma_t<SCHEME_REF, false, true>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_REF, false, false>(p, m, grid, first, s);
     }
-    if (vel) return launch_tma_t<SCHEME_KSPACE, true, false>(p, m, grid, s);
-    return launch_tma_t<SCHEME_KSPACE, false, false>(p, m, grid, s);
+    if (vel) return launch_tma_t<SCHEME_KSPACE, true, false>(p, m, grid, first, s);
+    return launch_tma_t<SCHEME_KSPACE, false, false>(p, m, grid, first, s);
 }
 
 }  // namespace bt

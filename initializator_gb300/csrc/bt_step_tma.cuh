@@ -142,7 +142,7 @@ __global__ void cell_velocity_kernel(const StepParams<float> P, float* __restric
 
 template <int SCHEME, bool VEL, bool PREC>
 __global__ void __launch_bounds__(tma::NT, 2)
-    step_tma_kernel(const __grid_constant__ StepParams<float> P, const __grid_constant__ TmaMaps M) {
+    step_tma_kernel(const __grid_constant__ StepParams<float> P, const __grid_constant__ TmaMaps M, int first) {
     using namespace tma;
     // TMA destinations must sit on 128-byte boundaries: align the dynamic
     // shared-memory base explicitly (the launch reserves 128 spare bytes)
@@ -223,7 +223,13 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // visible (returns at once when this launch has no programmatic
     // dependency)
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    const long long step = __ldcg(&P.ctl->step);
+    // the step index: from Ctl::step for the first step of a run of fast
+    // steps, else from this side's slot, which the previous step's CTA 0
+    // wrote; CTA 0 writes the other side's slot for the next step (read only
+    // after this grid has completed, so no CTA of this step sees it change)
+    const bool cta0 = (blockIdx.x | blockIdx.y | blockIdx.z) == 0;
+    const long long step = first ? __ldcg(&P.ctl->step) : __ldcg(&P.ctl->fstep[P.side]);
+    if (cta0 && tid == 0) P.ctl->fstep[1 - P.side] = step + 1;
     const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched) * nb + b;
     if (tid == 0)
         for (int q = 0; q < NSTAGE && q < nplanes; ++q) {
@@ -239,6 +245,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
         for (int q = (tid + NT - (TW + TH)) % NT; q < z1 - z0; q += NT)
             lab_phase<float>(si->knext[2], z0 + q, P.dzd, s_ez[q].x, s_ez[q].y);
     }
+    // CTA 0 adds the previous step's partials (complete: that grid has
+    // finished) into its M(t) row while its own first planes are in flight
+    const unsigned nb_per = (unsigned)P.zsplit * gridDim.y * gridDim.z;
+    if (cta0 && !first) reduce_members<float>(P, P.partials_prev, step - 1, nb_per, red);
     __syncthreads();
     float exr[QX] = {1.f, 1.f, 1.f, 1.f}, exi[QX] = {0.f, 0.f, 0.f, 0.f};
     if constexpr (SCHEME == SCHEME_KSPACE) {
@@ -508,7 +518,6 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // ---- deterministic M(t) reduction (as step_kernel) ----
     {
         const unsigned local = (unsigned)zc + (unsigned)P.zsplit * (blockIdx.y + gridDim.y * blockIdx.z);
-        const unsigned nb_per = (unsigned)P.zsplit * gridDim.y * gridDim.z;
         cta_partial_acc(P, b, local, nb_per, acc, red);
     }
     return;
