@@ -524,7 +524,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-qsweep", action="store_true", help="skip the batched 32-gradient q-sweep (C3a) leg")
     ap.add_argument("--no-ragged", action="store_true", help="skip the 48-sample ragged batch (C3b) leg")
-    ap.add_argument("--c5", action="store_true", help="add the 1024x1024x768 (C5, ~30 GB) leg")
+    ap.add_argument("--c5", action="store_true", help="add the 1024x1024x768 (C5, ~40 GB) leg")
     ap.add_argument("--zsplit", type=int, default=0, help="fixed z-chunking of the fast path (skips the autotuner)")
     ap.add_argument("--profile", action="store_true",
                     help="device-resident phase only (for ncu captures); prints no bench line")
