@@ -16,9 +16,13 @@
 //     / above) rolls through registers;
 //   * the stencil is evaluated as relaxation + sum over the six faces of
 //     w_f * (M_f - M_0), w_f folding harmonic-mean diffusion and first-order
-//     upwind advection, with w_f = 0 on domain faces (copy ghosts give a zero
-//     difference in the reference, cpp:1664-1754) — FP32 only; the FP64 path
-//     keeps the reference's exact operation order in step_kernel;
+//     upwind advection; on a domain face the neighbour is the reference's
+//     copy ghost (cpp:1664-1754), the voxel itself (rotated by the face phase
+//     in the k frame), set once per plane in the few threads holding such a
+//     face, so the face contributes nothing up to FP32 rounding and no
+//     per-voxel weight zeroing is needed — FP32 only; the FP64 path keeps the
+//     reference's exact operation order (and exact zero weights) in
+//     step_kernel;
 //   * the advection enters through one value per voxel and axis,
 //     u = dt/(2 d) (v_lo + v_hi), zeroed where the face it draws from (v_hi
 //     for u < 0, v_lo for u > 0) is closed; cell_velocity_kernel forms it once
@@ -282,9 +286,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
         if (xb + i < nx && xb + i >= P.box[0] && xb + i < P.box[1]) xmask |= 1u << i;
     const bool row_sum = y < ny && y >= P.box[2] && y < P.box[3];
     const bool row_ok = y < ny;
-    // threads holding a domain face in x or y take the slow path that zeroes
-    // the weight of that face (the copy ghost gives a zero difference)
-    const bool xy_edge = (xb == 0) || (xb + QX >= nx) || (y == 0) || (y == ny - 1);
+    // threads holding a voxel on a domain face in x (lane 0 of the first
+    // tile, the thread holding x = nx - 1); rows on a face in y are warp-uniform
+    const bool x_lo = xb == 0;
+    const bool x_hi = xb <= nx - 1 && nx - 1 < xb + QX;
 
     Acc<float> acc[3];
     float prv[3][QX], cur[3][QX], nxt[3][QX];
@@ -346,6 +351,26 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
     }
 
+    // the value a domain face's ghost must hold for the face to contribute
+    // nothing (the reference's copy ghosts, cpp:1664-1754): the voxel itself,
+    // in the k frame rotated so that the stencil's face phase (exp(+i th) on
+    // the lower face, its conjugate on the upper) brings it back to the voxel
+    auto ghost = [&](float& gr, float& gi, float& gz, float mr, float mi, float mz, int a, bool upper) {
+        if constexpr (SCHEME == SCHEME_KSPACE) {
+            const float c = ph[a][0], s = upper ? -ph[a][1] : ph[a][1];
+            gr = c * mr + s * mi;
+            gi = c * mi - s * mr;
+        } else {
+            gr = mr;
+            gi = mi;
+        }
+        gz = mz;
+    };
+    auto ghost_plane = [&](float (&g)[3][QX], int a, bool upper) {
+#pragma unroll
+        for (int i = 0; i < QX; ++i) ghost(g[0][i], g[1][i], g[2][i], cur[0][i], cur[1][i], cur[2][i], a, upper);
+    };
+
     for (int q = 1; live && q + 1 < nplanes; ++q) {
         const int z = plane_of(q);
         const int sc = q % NSTAGE;
@@ -378,6 +403,23 @@ __global__ void __launch_bounds__(tma::NT, 2)
 #pragma unroll
             for (int i = 0; i < QX - 1; ++i) xp[c][i] = cur[c][i + 1];
         }
+        // voxels on a domain face in x or y: the halo value beyond the face
+        // (zero-filled by the copy) becomes the face's ghost, so no weight
+        // needs zeroing per voxel
+        if (x_lo) ghost(xm[0][0], xm[1][0], xm[2][0], cur[0][0], cur[1][0], cur[2][0], 0, false);
+        if (x_hi) {
+#pragma unroll
+            for (int i = 0; i < QX; ++i)
+                if (xb + i == nx - 1) ghost(xp[0][i], xp[1][i], xp[2][i], cur[0][i], cur[1][i], cur[2][i], 0, true);
+        }
+        if (y == 0) {
+#pragma unroll
+            for (int i = 0; i < QX; ++i) ghost(ym[0][i], ym[1][i], ym[2][i], cur[0][i], cur[1][i], cur[2][i], 1, false);
+        }
+        if (y == ny - 1) {
+#pragma unroll
+            for (int i = 0; i < QX; ++i) ghost(yp[0][i], yp[1][i], yp[2][i], cur[0][i], cur[1][i], cur[2][i], 1, true);
+        }
         const uint32_t code4 = *reinterpret_cast<const uint32_t*>(base + OFF_CODE + w * TW + QX * lane);
         float ux[QX] = {0.f, 0.f, 0.f, 0.f}, uy[QX] = {0.f, 0.f, 0.f, 0.f}, uz[QX] = {0.f, 0.f, 0.f, 0.f};
         if constexpr (VEL) {
@@ -389,7 +431,6 @@ __global__ void __launch_bounds__(tma::NT, 2)
             uy[0] = b.x; uy[1] = b.y; uy[2] = b.z; uy[3] = b.w;
             uz[0] = c.x; uz[1] = c.y; uz[2] = c.z; uz[3] = c.w;
         }
-        const bool edge = xy_edge || z == 0 || z == nz - 1;
         const uint32_t smask = (row_sum && z >= P.box[4] && z < P.box[5]) ? xmask : 0u;
         float o[3][QX];
         float sx_r = 0.f, sx_i = 0.f, sz_ = 0.f;  // this plane's sums over the 4 voxels
@@ -408,15 +449,6 @@ __global__ void __launch_bounds__(tma::NT, 2)
                 wym += fmaxf(uy[i], 0.f);
                 wzp -= fminf(uz[i], 0.f);
                 wzm += fmaxf(uz[i], 0.f);
-            }
-            if (edge) {
-                const int x = xb + i;
-                if (x == 0) wxm = 0.f;
-                if (x >= nx - 1) wxp = 0.f;
-                if (y == 0) wym = 0.f;
-                if (y >= ny - 1) wyp = 0.f;
-                if (z == 0) wzm = 0.f;
-                if (z == nz - 1) wzp = 0.f;
             }
             const float wsum = ((wxm + wxp) + (wym + wyp)) + (wzm + wzp);
             const float px0 = cur[0][i], py0 = cur[1][i], pz0 = cur[2][i];
@@ -494,6 +526,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
                 *reinterpret_cast<float4*>(P.out[c] + off) = make_float4(o[c][0], o[c][1], o[c][2], o[c][3]);
         }
         };
+        // planes on a domain face in z: the ghost plane beyond it (zero-filled
+        // by the copy, used by nothing else) becomes the face's ghost
+        if (z == 0) ghost_plane(d > 0 ? prv : nxt, 2, false);
+        if (z == nz - 1) ghost_plane(d > 0 ? nxt : prv, 2, true);
         if (d > 0) body(prv, nxt);
         else body(nxt, prv);
         release(q);
