@@ -332,6 +332,7 @@ class Solver:
         """torch views (3 x [nz][ny][nx], strided by the pitch) of the current
         field on the device (k frame for KSPACE); valid until the next run."""
         import torch
+        self.synchronize()  # the field is complete before other streams see it
         ptrs = [ctypes.c_void_p() for _ in range(3)]
         pitch = ctypes.c_int(0)
         self._check(self._l.bt_field_device(self._h, member, *[ctypes.byref(p) for p in ptrs], ctypes.byref(pitch)),

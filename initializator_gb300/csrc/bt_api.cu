@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/bt.h"
@@ -48,7 +49,8 @@ struct bt_handle {
     uint8_t* code = nullptr;
     void* vel[3] = {};
     float* ucell = nullptr;       // fast path: gated cell velocities [axis][z][y][pitch]
-    void* staging = nullptr;      // pinned host buffer, one component in the handle's precision
+    void* staging = nullptr;      // pinned host buffer: two halves of one component each (FP32 handles)
+    cudaEvent_t stage_ev[2] = {}; // the last copy through each half
     bt::StepInfo* steps_d = nullptr;
     long long nsched = 0;
     std::vector<bt::StepInfo> steps_h;
@@ -531,31 +533,74 @@ bool any_phase(const bt_handle* h) {
 }
 
 // dense [nz][ny][nx] host component <-> pitched device component
-int put_component(bt_handle* h, void* dst, const double* src) {
+// dst[q] = src[q] (a precision conversion) for q < n, over the host's cores
+// when the field is large, so that the host side of a transfer keeps up with
+// the copy engine
+template <typename D, typename S>
+void convert(D* dst, const S* src, size_t n) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = (unsigned)std::max<size_t>(1, std::min<size_t>(std::min(hw, 32u), n >> 20));
+    auto part = [dst, src, n, nt](unsigned t) {
+        const size_t a = n * t / nt, b = n * (t + 1) / nt;
+        for (size_t q = a; q < b; ++q) dst[q] = (D)src[q];
+    };
+    if (nt == 1) {
+        part(0);
+        return;
+    }
+    std::vector<std::thread> ts;
+    ts.reserve(nt - 1);
+    for (unsigned t = 1; t < nt; ++t) ts.emplace_back(part, t);
+    part(0);
+    for (auto& t : ts) t.join();
+}
+
+// host FP64 component -> device field. FP32 handles convert into staging half
+// `half` (once the previous copy out of it has finished) and copy from there,
+// so consecutive components alternate halves and each conversion overlaps the
+// previous component's copy
+int put_component(bt_handle* h, void* dst, const double* src, int half) {
     const bt_config& c = h->cfg;
     const size_t rows = (size_t)c.ny * c.nz;
     if (h->esz == 8) {
         CK(h, cudaMemcpy2DAsync(dst, h->pitch * 8, src, c.nx * 8, c.nx * 8, rows, cudaMemcpyHostToDevice, h->stream));
     } else {
-        CK(h, cudaStreamSynchronize(h->stream));  // the staging buffer may still feed a copy
-        float* f = static_cast<float*>(h->staging);
-        for (size_t q = 0; q < h->nvox; ++q) f[q] = (float)src[q];
+        float* f = static_cast<float*>(h->staging) + (size_t)half * h->nvox;
+        CK(h, cudaEventSynchronize(h->stage_ev[half]));
+        convert(f, src, h->nvox);
         CK(h, cudaMemcpy2DAsync(dst, h->pitch * 4, f, c.nx * 4, c.nx * 4, rows, cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaEventRecord(h->stage_ev[half], h->stream));
     }
     return BT_OK;
 }
 
-int get_component(bt_handle* h, double* dst, const void* src) {
+// device field components -> host FP64 (n of them): for FP32 handles the copy
+// of component i + 1 into one staging half runs while component i is
+// converted out of the other
+int get_components(bt_handle* h, double* const* dst, const void* const* src, int n) {
     const bt_config& c = h->cfg;
     const size_t rows = (size_t)c.ny * c.nz;
     if (h->esz == 8) {
-        CK(h, cudaMemcpy2DAsync(dst, c.nx * 8, src, h->pitch * 8, c.nx * 8, rows, cudaMemcpyDeviceToHost, h->stream));
+        for (int i = 0; i < n; ++i)
+            CK(h, cudaMemcpy2DAsync(dst[i], c.nx * 8, src[i], h->pitch * 8, c.nx * 8, rows, cudaMemcpyDeviceToHost,
+                                    h->stream));
         CK(h, cudaStreamSynchronize(h->stream));
-    } else {
-        float* f = static_cast<float*>(h->staging);
-        CK(h, cudaMemcpy2DAsync(f, c.nx * 4, src, h->pitch * 4, c.nx * 4, rows, cudaMemcpyDeviceToHost, h->stream));
-        CK(h, cudaStreamSynchronize(h->stream));
-        for (size_t q = 0; q < h->nvox; ++q) dst[q] = (double)f[q];
+        return BT_OK;
+    }
+    float* f = static_cast<float*>(h->staging);
+    for (int i = 0; i <= n; ++i) {
+        if (i < n) {
+            // the half was last read by the conversion of component i - 2, done by now
+            float* fi = f + (size_t)(i & 1) * h->nvox;
+            CK(h, cudaMemcpy2DAsync(fi, c.nx * 4, src[i], h->pitch * 4, c.nx * 4, rows, cudaMemcpyDeviceToHost,
+                                    h->stream));
+            CK(h, cudaEventRecord(h->stage_ev[i & 1], h->stream));
+        }
+        if (i > 0) {
+            const int j = i - 1;
+            CK(h, cudaEventSynchronize(h->stage_ev[j & 1]));
+            convert(dst[j], f + (size_t)(j & 1) * h->nvox, h->nvox);
+        }
     }
     return BT_OK;
 }
@@ -631,7 +676,11 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
             cudaMemset(h->ucell, 0, sizeof(float) * 3 * h->comp);
         }
     }
-    if (cfg->precision == BT_F32 && cudaMallocHost(&h->staging, 4 * h->nvox) != cudaSuccess) return bail(BT_E_NOMEM);
+    if (cfg->precision == BT_F32) {
+        if (cudaMallocHost(&h->staging, 2 * 4 * h->nvox) != cudaSuccess) return bail(BT_E_NOMEM);
+        for (auto& e : h->stage_ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bail(BT_E_CUDA);
+    }
     if (cfg->batch < 0 || (long long)h->nb * (long long)h->comp * 3 > (1LL << 40)) return bail(BT_E_ARG);
     const size_t nblocks = (size_t)h->grid.x * h->grid.y * h->grid.z;
     h->partials_cap = std::max<size_t>(3 * nblocks, 4 * SUMS_BLOCKS);
@@ -668,6 +717,8 @@ int bt_destroy(bt_handle* h) {
     if (h->ctl_d) cudaFree(h->ctl_d);
     if (h->ctl_h) cudaFreeHost(h->ctl_h);
     if (h->staging) cudaFreeHost(h->staging);
+    for (auto& e : h->stage_ev)
+        if (e) cudaEventDestroy(e);
     if (h->partials_d) cudaFree(h->partials_d);
     if (h->mt_d) cudaFree(h->mt_d);
     if (h->fields_d) cudaFree(h->fields_d);
@@ -734,13 +785,12 @@ int bt_set_state(bt_handle* h, const double* mx, const double* my, const double*
     for (int b = 0; b < h->nb; ++b)
         for (int a = 0; a < 3; ++a) {
             void* dst = (char*)h->state[h->cur][a] + (size_t)b * 3 * h->comp * h->esz;
-            int rc = put_component(h, dst, src[a] + (size_t)b * h->nvox);
+            int rc = put_component(h, dst, src[a] + (size_t)b * h->nvox, (3 * b + a) & 1);
             if (rc) return rc;
         }
-    int rc = frame_change(h, h->state[h->cur], +1);
-    if (rc) return rc;
-    CK(h, cudaStreamSynchronize(h->stream));
-    return BT_OK;
+    // the host arrays have been read (converted into the staging halves); the
+    // copies and the frame change complete in the handle's stream order
+    return frame_change(h, h->state[h->cur], +1);
 }
 
 int bt_set_state_device(bt_handle* h, const void* mx, const void* my, const void* mz) {
@@ -770,13 +820,14 @@ int bt_get_state(bt_handle* h, double* mx, double* my, double* mz) {
     }
     double* dst[3] = {mx, my, mz};
     void** from = phase ? tmp : src;
+    std::vector<double*> to;
+    std::vector<const void*> fr;
     for (int b = 0; b < h->nb; ++b)
         for (int a = 0; a < 3; ++a) {
-            int rc = get_component(h, dst[a] + (size_t)b * h->nvox,
-                                   (const char*)from[a] + (size_t)b * 3 * h->comp * h->esz);
-            if (rc) return rc;
+            to.push_back(dst[a] + (size_t)b * h->nvox);
+            fr.push_back((const char*)from[a] + (size_t)b * 3 * h->comp * h->esz);
         }
-    return BT_OK;
+    return get_components(h, to.data(), fr.data(), (int)to.size());
 }
 
 int bt_set_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const double* grad_wave, long long nwave) {
