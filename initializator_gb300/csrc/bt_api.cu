@@ -788,9 +788,14 @@ int bt_set_state(bt_handle* h, const double* mx, const double* my, const double*
             int rc = put_component(h, dst, src[a] + (size_t)b * h->nvox, (3 * b + a) & 1);
             if (rc) return rc;
         }
-    // the host arrays have been read (converted into the staging halves); the
-    // copies and the frame change complete in the handle's stream order
-    return frame_change(h, h->state[h->cur], +1);
+    // FP32: the host arrays have been read (converted into the staging
+    // halves); the copies and the frame change complete in the handle's
+    // stream order. FP64 copies read the caller's arrays directly, so they
+    // finish before the call returns.
+    int rc = frame_change(h, h->state[h->cur], +1);
+    if (rc) return rc;
+    if (h->esz == 8) CK(h, cudaStreamSynchronize(h->stream));
+    return BT_OK;
 }
 
 int bt_set_state_device(bt_handle* h, const void* mx, const void* my, const void* mz) {

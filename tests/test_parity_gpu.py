@@ -161,6 +161,30 @@ def test_kspace_state_roundtrip_mid_gradient(btlib):
         assert rel_err(s.measure(), x.sum(axis=(1, 2, 3))) < 1e-12
 
 
+def test_f32_state_transfer_pipeline(btlib):
+    """FP32 host transfers convert each component on the host's cores into one
+    of two pinned staging halves, alternating halves: a batch of 3 fields (9
+    components, so both halves are reused) read back right after set_state is
+    the FP32 rounding of the input, member by member; a second set_state at
+    once (its halves wait for the first one's copies) leaves the second input;
+    the field (2^21 voxels) is large enough for the conversion to use several
+    threads."""
+    import initializator_gb300 as bt
+    shape = (32, 256, 256)
+    mask = np.ones(shape, np.uint8)
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((3, 3) + shape)
+    b = rng.standard_normal((3, 3) + shape)
+    with bt.Solver(bt.make_config(shape, dx=1e-6, dt=1e-6, precision=bt.BT_F32, batch=3)) as s:
+        s.upload_geometry(mask, None)
+        s.set_state(a)
+        got = s.get_state()
+        assert np.array_equal(got, a.astype(np.float32).astype(np.float64))
+        s.set_state(a)
+        s.set_state(b)
+        assert np.array_equal(s.get_state(), b.astype(np.float32).astype(np.float64))
+
+
 def test_determinism_and_graph_equivalence(btlib):
     import initializator_gb300 as bt
     shape = (30, 41, 70)
