@@ -175,8 +175,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
     const unsigned b = blockIdx.x % nb;
     const int zc = (int)(blockIdx.x / nb);
     const int x0 = blockIdx.y * TW, y0 = blockIdx.z * TH;
-    const int z0 = zc * P.zchunk;
-    const int z1 = min(nz, z0 + P.zchunk);
+    // even chunks (lengths differ by at most one plane), so the CTAs of the
+    // last wave end together
+    const int z0 = (int)((long long)zc * nz / P.zsplit);
+    const int z1 = (int)((long long)(zc + 1) * nz / P.zsplit);
     const int d = (zc & 1) ? -1 : 1;
     const int xb = x0 + QX * lane;  // first of this thread's 4 voxels
     const int y = y0 + w;
