@@ -306,30 +306,33 @@ __global__ void __launch_bounds__(tma::NT, 2)
     };
     // s_flags[0] is the CTA's failure flag (volatile: polled inside waits)
     volatile int* vflag = s_flags;
-    // warp-uniform bounded wait for plane q's copy; false when it gave up or
-    // another thread of the CTA raised the failure flag
-    auto wait_full = [&](int q) -> bool {
-        const uint32_t par = (uint32_t)(q / NSTAGE) & 1u;
+    // Plane q of the sequence uses slot q % NSTAGE for the (q / NSTAGE)-th
+    // time, so its full barrier completes phase (q / NSTAGE) & 1; the loop
+    // carries slot and parity instead of dividing.
+    // warp-uniform bounded wait for the copy into `slot` at phase parity
+    // `par`; false when it gave up or another thread of the CTA raised the
+    // failure flag
+    auto wait_full = [&](int slot, uint32_t par) -> bool {
         for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
-            if (__all_sync(0xffffffffu, mbar_try_wait(&bars[q % NSTAGE], par))) return true;
+            if (__all_sync(0xffffffffu, mbar_try_wait(&bars[slot], par))) return true;
             if (__any_sync(0xffffffffu, vflag[0] != 0)) return false;
         }
         if (lane == 0) vflag[0] = 1;
         return false;
     };
-    // a warp is done with plane q's slot
-    auto release = [&](int q) {
+    // a warp is done with a slot
+    auto release = [&](int slot) {
         __syncwarp();
-        if (lane == 0) mbar_arrive(&empties[q % NSTAGE]);
+        if (lane == 0) mbar_arrive(&empties[slot]);
     };
-    // producer (thread 0): plane p into slot p % NSTAGE once every warp has
-    // released plane p - NSTAGE from it (bounded; raises the flag on timeout)
-    auto refill = [&](int p) {
-        const uint32_t par = (uint32_t)((p - NSTAGE) / NSTAGE) & 1u;
+    // producer (thread 0): plane p into `slot` (= p % NSTAGE) once every warp
+    // has released plane p - NSTAGE from it, whose phase parity is `par`
+    // (bounded; raises the flag on timeout)
+    auto refill = [&](int p, int slot, uint32_t par) {
         for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
-            if (mbar_try_wait(&empties[p % NSTAGE], par)) {
+            if (mbar_try_wait(&empties[slot], par)) {
                 fence_proxy_async();
-                issue(p % NSTAGE, plane_of(p));
+                issue(slot, plane_of(p));
                 n_issued++;
                 return;
             }
@@ -341,15 +344,15 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // prologue: the ghost-side plane (q = 0) and the first plane (q = 1)
     bool live = !empty;
     if (live) {
-        live = wait_full(0);
+        live = wait_full(0, 0u);
         if (live) {
             own(0, prv);
-            live = wait_full(1);
+            live = wait_full(1, 0u);
         }
         if (live) {
             own(1, cur);
             release(0);
-            if (tid == 0 && nplanes > NSTAGE) refill(NSTAGE);
+            if (tid == 0 && nplanes > NSTAGE) refill(NSTAGE, 0, 0u);
         }
     }
 
@@ -373,11 +376,15 @@ __global__ void __launch_bounds__(tma::NT, 2)
         for (int i = 0; i < QX; ++i) ghost(g[0][i], g[1][i], g[2][i], cur[0][i], cur[1][i], cur[2][i], a, upper);
     };
 
+    // output offset of this thread's row in plane 0
+    const long long obase = (long long)b * P.bstride + (long long)y * P.pitch + xb;
+    int sc = 1;         // slot of plane q
+    uint32_t pc = 0u;   // its phase parity
     for (int q = 1; live && q + 1 < nplanes; ++q) {
         const int z = plane_of(q);
-        const int sc = q % NSTAGE;
-        if (!wait_full(q + 1)) break;
-        const int sn = (q + 1) % NSTAGE;
+        const int sn = sc == NSTAGE - 1 ? 0 : sc + 1;   // slot of plane q + 1
+        const uint32_t pn = sc == NSTAGE - 1 ? pc ^ 1u : pc;
+        if (!wait_full(sn, pn)) break;
         own(sn, nxt);
         // one instance of the plane body per marching direction, so that
         // below / above bind to fixed registers
@@ -522,7 +529,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
         acc[2].add(sz_);
         if (row_ok && xb < nx) {
-            const long long off = (long long)b * P.bstride + (long long)z * P.plane + (long long)y * P.pitch + xb;
+            const long long off = obase + (long long)z * P.plane;
 #pragma unroll
             for (int c = 0; c < 3; ++c)
                 *reinterpret_cast<float4*>(P.out[c] + off) = make_float4(o[c][0], o[c][1], o[c][2], o[c][3]);
@@ -534,8 +541,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
         if (z == nz - 1) ghost_plane(d > 0 ? nxt : prv, 2, true);
         if (d > 0) body(prv, nxt);
         else body(nxt, prv);
-        release(q);
-        if (tid == 0 && q + NSTAGE < nplanes) refill(q + NSTAGE);
+        release(sc);
+        if (tid == 0 && q + NSTAGE < nplanes) refill(q + NSTAGE, sc, pc);
+        sc = sn;
+        pc = pn;
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
