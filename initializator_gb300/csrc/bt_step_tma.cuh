@@ -380,8 +380,12 @@ __global__ void __launch_bounds__(tma::NT, 2)
     const long long obase = (long long)b * P.bstride + (long long)y * P.pitch + xb;
     int sc = 1;         // slot of plane q
     uint32_t pc = 0u;   // its phase parity
-    for (int q = 1; live && q + 1 < nplanes; ++q) {
-        const int z = plane_of(q);
+    // M(t) summation mask: fixed for the whole chunk unless the trimming box
+    // cuts it in z (never for the default box)
+    const uint32_t smask_row = row_sum ? xmask : 0u;
+    const bool z_trim = !(z0 >= P.box[4] && z1 <= P.box[5]);
+    int z = plane_of(1);
+    for (int q = 1; live && q + 1 < nplanes; ++q, z += d) {
         const int sn = sc == NSTAGE - 1 ? 0 : sc + 1;   // slot of plane q + 1
         const uint32_t pn = sc == NSTAGE - 1 ? pc ^ 1u : pc;
         if (!wait_full(sn, pn)) break;
@@ -440,7 +444,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
             uy[0] = b.x; uy[1] = b.y; uy[2] = b.z; uy[3] = b.w;
             uz[0] = c.x; uz[1] = c.y; uz[2] = c.z; uz[3] = c.w;
         }
-        const uint32_t smask = (row_sum && z >= P.box[4] && z < P.box[5]) ? xmask : 0u;
+        uint32_t smask = smask_row;
+        if (z_trim && (z < P.box[4] || z >= P.box[5])) smask = 0u;
         float o[3][QX];
         float sx_r = 0.f, sx_i = 0.f, sz_ = 0.f;  // this plane's sums over the 4 voxels
 #pragma unroll
