@@ -184,8 +184,14 @@ def run_ragged(args, lr):
     torch.cuda.synchronize()
     t_many = time.perf_counter() - t0
     finite = all(bool(np.all(np.isfinite(m))) for m in mts)
+    # one sample after another, each with the chunking it would take alone
+    # (run_many set the chunking for sharing the GPU); warm-up recaptures
     for s in solvers:
+        s.set_zsplit(0)
         s.set_step(0)
+        s.run(64)
+        s.set_step(0)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in solvers:
         s.run(RAGGED_STEPS)

@@ -175,8 +175,9 @@ int bt_read_mt_phases(bt_handle* h, double* out, long long nsteps);
  * geometry and schedule) by nsteps each, asynchronously. Launches are
  * interleaved round robin, one captured graph of steps per handle per round,
  * so small grids on the handles' separate streams run side by side on the
- * GPU. Read each handle's M(t) with bt_read_mt. No reference counterpart: the
- * reference runs one sample per process (main.cpp:34-36). */
+ * GPU; the handles' FP32 fast paths get z-chunks for sharing the GPU (see
+ * bt_set_tma_split). Read each handle's M(t) with bt_read_mt. No reference
+ * counterpart: the reference runs one sample per process (main.cpp:34-36). */
 int bt_run_many(bt_handle* const* hs, int n, long long nsteps);
 int bt_read_mt(bt_handle* h, double* mt_out, long long nsteps);
 int bt_synchronize(bt_handle* h);
@@ -191,6 +192,13 @@ int bt_measure(bt_handle* h, double* sums3);
  * thread per voxel, cu:1475-1476). The field and step index are restored.
  * *best_zsplit (may be NULL) receives the chosen split. */
 int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit);
+
+/* The FP32 fast path's z-chunking: zsplit chunks per column (<= 0: the
+ * default for a handle running alone, about four waves of CTAs). A no-op for
+ * handles without the fast path. bt_run_many sets the chunking of its handles
+ * for sharing the GPU (about four waves over all of them together); this call
+ * (or bt_autotune) sets it back for running alone. */
+int bt_set_tma_split(bt_handle* h, int zsplit);
 
 /* Device pointers of the current field of batch member `member` (no
  * reference counterpart: the learned closure corrects the field in place).

@@ -69,7 +69,7 @@ EXPORTS = [
     "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
     "bt_run_many", "bt_read_mt", "bt_synchronize", "bt_upload_rates", "bt_set_phase_weights",
     "bt_read_mt_phases", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
-    "bt_version", "bt_autotune", "bt_step_noalloc",
+    "bt_version", "bt_autotune", "bt_set_tma_split", "bt_step_noalloc",
     "bt_conv3d_margin", "bt_conv3d", "bt_conv3d_weight_grad", "bt_conv3d_wgrad_scratch", "bt_conv3d_pack_weights",
     "bt_adamw", "bt_umma_selftest", "bt_field_device",
 ]
@@ -113,6 +113,7 @@ def lib():
                                   ctypes.POINTER(ctypes.c_int)], i),
         "bt_version": ([], ctypes.c_char_p),
         "bt_autotune": ([vp, i, ctypes.POINTER(ctypes.c_int)], i),
+        "bt_set_tma_split": ([vp, i], i),
         "bt_step_noalloc": ([ctypes.POINTER(Config), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
         "bt_conv3d_margin": ([i, i], ll),
         "bt_conv3d": ([ctypes.POINTER(Conv3dArgs), vp], i),
@@ -327,6 +328,11 @@ class Solver:
         best = ctypes.c_int(0)
         self._check(self._l.bt_autotune(self._h, int(trial_steps), ctypes.byref(best)), "autotune")
         return best.value
+
+    def set_zsplit(self, zsplit=0):
+        """The FP32 fast path's z-chunks per column (0: the default for running
+        alone; run_many sets them for sharing the GPU)."""
+        self._check(self._l.bt_set_tma_split(self._h, int(zsplit)), "set_tma_split")
 
     def field_views(self, member=0):
         """torch views (3 x [nz][ny][nx], strided by the pitch) of the current

@@ -293,6 +293,9 @@ int normalise_split(int nz, int zsplit) {
 int set_tma_split(bt_handle* h, int zsplit) {
     const bt_config& c = h->cfg;
     zsplit = normalise_split(c.nz, zsplit);
+    // unchanged since the last call (tpart is only ever set here): keep the
+    // captured graphs
+    if (zsplit == h->tzsplit && h->tpart > 0) return BT_OK;
     const int gx = (c.nx + bt::TMA_TX - 1) / bt::TMA_TX, gy = (c.ny + bt::TMA_TY - 1) / bt::TMA_TY;
     h->tzsplit = zsplit;
     h->tgrid = dim3(zsplit * h->nb, gx, gy);
@@ -932,6 +935,29 @@ int bt_run_many(bt_handle* const* hs, int n, long long nsteps) {
     if (!hs || n < 0 || nsteps < 0) return BT_E_ARG;
     for (int i = 0; i < n; ++i)
         if (!hs[i]) return BT_E_ARG;
+    // the handles share the GPU: their fast paths get z-chunks such that all
+    // of them together launch about four waves of two CTAs per SM, each
+    // handle's share in proportion to its voxels (a handle alone would take
+    // four waves by itself, and many short chunks pay many CTA prologues)
+    if (n > 1) {
+        long long vox_all = 0;
+        for (int i = 0; i < n; ++i)
+            if (hs[i]->use_tma) vox_all += (long long)hs[i]->nvox * hs[i]->nb;
+        for (int i = 0; i < n && vox_all > 0; ++i) {
+            bt_handle* h = hs[i];
+            if (!h->use_tma) continue;
+            const bt_config& c = h->cfg;
+            const double tiles =
+                (double)((c.nx + bt::TMA_TX - 1) / bt::TMA_TX) * ((c.ny + bt::TMA_TY - 1) / bt::TMA_TY) * h->nb;
+            const double want = 8.0 * h->num_sms * ((double)h->nvox * h->nb / (double)vox_all) / tiles;
+            const int zs = (int)std::max(1.0, std::min(std::floor(want + 0.5), (double)std::max(1, c.nz / 8)));
+            if (zs != h->tzsplit) {
+                CK(h, cudaStreamSynchronize(h->stream));
+                int rc = set_tma_split(h, zs);
+                if (rc) return rc;
+            }
+        }
+    }
     for (int i = 0; i < n; ++i) {
         int rc = run_begin(hs[i], nsteps);
         if (rc) return rc;
@@ -1131,6 +1157,13 @@ int bt_field_device(bt_handle* h, int member, void** mx, void** my, void** mz, i
     *mz = (char*)h->state[h->cur][2] + off;
     *pitch = h->pitch;
     return BT_OK;
+}
+
+int bt_set_tma_split(bt_handle* h, int zsplit) {
+    if (!h) return BT_E_ARG;
+    if (h->cfg.precision != BT_F32 || !h->use_tma) return BT_OK;  // no fast path on this handle
+    CK(h, cudaStreamSynchronize(h->stream));
+    return set_tma_split(h, zsplit > 0 ? zsplit : default_tma_split(h));
 }
 
 int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {

@@ -295,6 +295,43 @@ def test_tma_zsplits_and_autotune(btlib, monkeypatch):
         assert rel_err(s.get_state(), st0) <= 1e-7
         s.run(40)
         assert np.array_equal(s.get_state(), fields[0][0])
+    # the explicit setter, changed mid-run (0: the default for a handle alone)
+    with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, **kw)) as s:
+        s.upload_geometry(mask, vel)
+        s.set_state(st0)
+        s.set_zsplit(5)
+        mt_a = s.run(20)
+        s.set_zsplit(0)
+        mt_b = s.run(20)
+        assert np.array_equal(s.get_state(), fields[0][0])
+        assert rel_err(np.vstack([mt_a, mt_b]), fields[0][1]) <= 1e-6
+
+
+def test_ragged_shared_chunking(btlib):
+    """run_many gives handles that share the GPU longer z-chunks than each
+    would take alone (here 5 instead of 8 per column for eight 256 x 128 x 64
+    grids); fields stay bit-identical to each handle run alone and M(t) agrees
+    to 1e-6 (only the FP32 grouping of the per-thread sums changes)."""
+    import initializator_gb300 as bt
+    shape = (64, 128, 256)
+    cases = [_random_case(shape, seed=40 + i, prec=False) for i in range(8)]
+
+    def make(case):
+        mask, vel, st0, kw = case
+        s = bt.Solver(bt.make_config(shape, precision=bt.BT_F32, **kw))
+        s.upload_geometry(mask, vel)
+        s.set_state(st0)
+        return s
+
+    many = [make(c) for c in cases]
+    mts = bt.run_many(many, 40)
+    for s, c, mt in zip(many, cases, mts):
+        st = s.get_state()
+        s.close()
+        with make(c) as one:
+            mt1 = one.run(40)
+            assert np.array_equal(st, one.get_state())
+        assert rel_err(mt, mt1) <= 1e-6
 
 
 @pytest.mark.parametrize("precision", ["f32", "f64"])
