@@ -1,8 +1,10 @@
 // FP32 fast path of the fused step (K1, TMA form) for sm_103a.
 //
-// Same update, sums and step-counter protocol as step_kernel (bt_step.cuh),
-// for steps without pulses:
-//   * a CTA owns a 128 x 8 column tile and marches through a z-chunk;
+// Same update and M(t) as step_kernel (bt_step.cuh), for steps without pulses:
+//   * a CTA owns a 128 x 8 column tile and marches through a z-chunk (the
+//     column split into P.zsplit even chunks; odd chunks march downwards, so
+//     the plane two neighbouring chunks share is read by both at about the
+//     same moment and the second read hits L2);
 //   * each z-plane of the tile (the three field components with a one-voxel
 //     x/y halo, upwind cell velocities, geometry code) is fetched by one thread with
 //     cp.async.bulk.tensor into a 3-slot shared-memory ring, completion
@@ -28,13 +30,21 @@
 //     for u < 0, v_lo for u > 0) is closed; cell_velocity_kernel forms it once
 //     per geometry upload with the same FP32 operations the per-face form
 //     uses, so the weights are bit-identical to it and a plane's velocities
-//     are one 3 x 128 x 8 box instead of three face boxes with halos.
+//     are one 3 x 128 x 8 box instead of three face boxes with halos;
+//   * M(t) and the step counter: each CTA stores its FP64 partial (per-thread
+//     Kahan, per-warp float-float, per-CTA FP64) into the partials buffer of
+//     its input side; CTA 0 of the next fast step adds them in a fixed order
+//     while its first planes load, and step_finish_kernel does so for the last
+//     step of a run of fast steps. The first step of a run reads Ctl::step,
+//     later ones the counter slot of their input side (Ctl::fstep), which the
+//     previous step's CTA 0 wrote and which is read only after that grid has
+//     completed; no CTA waits on a fence or an atomic ticket.
 // Out-of-range TMA boxes (halo beyond the domain, plane -1 or nz) are
 // zero-filled and never used as data.
 // Every mbarrier wait is bounded; a wait that gives up raises the CTA's
 // failure flag, which ends the other warps' waits too; after the march the
 // CTA then records status bit 8, drains its copies (bounded) and returns
-// without touching the step counter.
+// without storing its partial.
 #pragma once
 #include "bt_step.cuh"
 
