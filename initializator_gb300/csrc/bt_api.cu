@@ -43,6 +43,7 @@ struct bt_handle {
     int nb = 1;                   // fields advanced together (batch members)
     int gzsplit = 1;              // z-chunks per field, generic kernel
     int tzsplit = 1;              // z-chunks per field, TMA kernel
+    int ttx = 128;                // tile width of the TMA kernel (128, or 64 for narrow grids)
     void* state_base[2] = {};     // one allocation per ping-pong side: [batch][component][z][y][pitch]
     void* state[2][3] = {};
     int cur = 0;
@@ -262,20 +263,20 @@ bool build_maps(bt_handle* h) {
         {
             cuuint64_t dims[5] = {nx, ny, nz, 3, (cuuint64_t)h->nb};
             cuuint64_t str[4] = {P4, P4 * ny, (cuuint64_t)h->comp * 4, (cuuint64_t)h->comp * 12};
-            cuuint32_t box[5] = {bt::TMA_TX + 8, bt::TMA_TY + 2, 1, 3, 1};
+            cuuint32_t box[5] = {(cuuint32_t)h->ttx + 8, (cuuint32_t)bt::tile_rows(h->ttx) + 2, 1, 3, 1};
             if (!encode(&M.state, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, h->state_base[s], dims, str, box)) return false;
         }
         {
             cuuint64_t dims[3] = {nx, ny, nz};
             cuuint64_t str[2] = {(cuuint64_t)h->cpitch, (cuuint64_t)h->cpitch * ny};
-            cuuint32_t box[3] = {bt::TMA_TX, bt::TMA_TY, 1};
+            cuuint32_t box[3] = {(cuuint32_t)h->ttx, (cuuint32_t)bt::tile_rows(h->ttx), 1};
             if (!encode(&M.code, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, h->code, dims, str, box)) return false;
         }
         if (c.velocity == 1) {
             if (!h->ucell) return false;
             cuuint64_t dims[4] = {nx, ny, nz, 3};
             cuuint64_t str[3] = {P4, P4 * ny, (cuuint64_t)h->comp * 4};
-            cuuint32_t box[4] = {bt::TMA_TX, bt::TMA_TY, 1, 3};
+            cuuint32_t box[4] = {(cuuint32_t)h->ttx, (cuuint32_t)bt::tile_rows(h->ttx), 1, 3};
             if (!encode(&M.ucell, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->ucell, dims, str, box)) return false;
         }
     }
@@ -296,7 +297,8 @@ int set_tma_split(bt_handle* h, int zsplit) {
     // unchanged since the last call (tpart is only ever set here): keep the
     // captured graphs
     if (zsplit == h->tzsplit && h->tpart > 0) return BT_OK;
-    const int gx = (c.nx + bt::TMA_TX - 1) / bt::TMA_TX, gy = (c.ny + bt::TMA_TY - 1) / bt::TMA_TY;
+    const int tw = h->ttx, th = bt::tile_rows(tw);
+    const int gx = (c.nx + tw - 1) / tw, gy = (c.ny + th - 1) / th;
     h->tzsplit = zsplit;
     h->tgrid = dim3(zsplit * h->nb, gx, gy);
     h->tpart = 3 * (size_t)zsplit * gx * gy * h->nb;
@@ -315,8 +317,8 @@ int set_tma_split(bt_handle* h, int zsplit) {
 // default split: about 4 waves of 2 CTAs per SM, chunks of at least 8 planes
 int default_tma_split(const bt_handle* h) {
     const bt_config& c = h->cfg;
-    const long long tiles =
-        (long long)((c.nx + bt::TMA_TX - 1) / bt::TMA_TX) * ((c.ny + bt::TMA_TY - 1) / bt::TMA_TY) * h->nb;
+    const int tw = h->ttx, th = bt::tile_rows(tw);
+    const long long tiles = (long long)((c.nx + tw - 1) / tw) * ((c.ny + th - 1) / th) * h->nb;
     const long long slots = 2LL * h->num_sms;
     long long zs = (4 * slots + tiles - 1) / tiles;
     zs = std::min<long long>(zs, std::max(1, c.nz / 8));
@@ -347,8 +349,8 @@ cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
     if (fast) {
         // a fast step after a fast step adds its predecessor's partials
         h->launches++;
-        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, !h->fast_pending,
-                                h->stream);
+        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, h->ttx,
+                                !h->fast_pending, h->stream);
         h->fast_pending = true;
         h->fast_side = side;
         // the two-component sums read Ctl::step
@@ -698,6 +700,10 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     rc = build_schedule(h, nullptr, 0, nullptr, 0);
     if (rc) return bail(rc);
     if (cfg->precision == BT_F32 && cfg->scheme != BT_SCHEME_MACCORMACK && !std::getenv("BT_NO_TMA")) {
+        // 64-wide tiles where they pad x less than 128-wide ones (narrow or
+        // odd widths); BT_TMA_TW = 64 / 128 forces one
+        h->ttx = ((cfg->nx + 63) / 64) * 64 < ((cfg->nx + 127) / 128) * 128 ? 64 : 128;
+        if (const char* e = std::getenv("BT_TMA_TW")) h->ttx = std::atoi(e) == 64 ? 64 : 128;
         rc = set_tma_split(h, default_tma_split(h));
         if (rc) return bail(rc);
     }
@@ -947,8 +953,8 @@ int bt_run_many(bt_handle* const* hs, int n, long long nsteps) {
             bt_handle* h = hs[i];
             if (!h->use_tma) continue;
             const bt_config& c = h->cfg;
-            const double tiles =
-                (double)((c.nx + bt::TMA_TX - 1) / bt::TMA_TX) * ((c.ny + bt::TMA_TY - 1) / bt::TMA_TY) * h->nb;
+            const int tw = h->ttx, th = bt::tile_rows(tw);
+            const double tiles = (double)((c.nx + tw - 1) / tw) * ((c.ny + th - 1) / th) * h->nb;
             const double want = 8.0 * h->num_sms * ((double)h->nvox * h->nb / (double)vox_all) / tiles;
             const int zs = (int)std::max(1.0, std::min(std::floor(want + 0.5), (double)std::max(1, c.nz / 8)));
             if (zs != h->tzsplit) {

@@ -125,13 +125,15 @@ cudaError_t launch_phase_sums(const StepParams<T>& p, const T* w1, const T* w2, 
 // into M(t); launch_tma_finish(last step's parameters) closes the run (the last
 // step's M(t), Ctl::step)
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
-                            bool first, cudaStream_t s);
+                            int tw, bool first, cudaStream_t s);
+cudaError_t launch_step_tma64(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
+                              bool first, cudaStream_t s);
 cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_t s);
-int tma_smem_bytes();
+int tma_smem_bytes(int tw);
 // upwind cell velocities of the fast path from the face velocities, [axis][z][y][pitch]
 cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s);
-constexpr int TMA_TX = 128;  // tile width (voxels along x) of the fast path
-constexpr int TMA_TY = 8;    // tile height (rows along y) of the fast path
+// tile of the fast path: tw = 128 or 64 voxels along x, tile_rows(tw) rows along y
+inline int tile_rows(int tw) { return tw == 64 ? 16 : 8; }
 template <typename T>
 cudaError_t launch_frame(T* f[3], const uint8_t* code, int nx, int ny, int nz, int pitch, int cpitch, double kx,
                          double ky, double kz, double dx, double dy, double dz, int sign, cudaStream_t s);

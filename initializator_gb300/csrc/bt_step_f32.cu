@@ -41,41 +41,11 @@ cudaError_t launch_frame<float>(float* f[3], const uint8_t* code, int nx, int ny
     return cudaGetLastError();
 }
 
-int tma_smem_bytes() { return tma::SMEM; }
+int tma_smem_bytes(int tw) { return tw == 64 ? tma::Tile<64>::SMEM : tma::Tile<128>::SMEM; }
 
 cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s) {
     cell_velocity_kernel<<<1216, 256, 0, s>>>(p, u, comp);
     return cudaGetLastError();
-}
-
-// programmatic dependent launch: a kernel overlaps its step-independent
-// prologue with the previous launch's tail (BT_NO_PDL turns it off)
-static cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, int smem, cudaStream_t s, cudaLaunchAttribute* attr) {
-    static const bool pdl = std::getenv("BT_NO_PDL") == nullptr;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = pdl ? 1 : 0;
-    return cfg;
-}
-
-template <int SCHEME, bool VEL, bool PREC>
-static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, bool first, cudaStream_t s) {
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, tma::SMEM);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
-    cudaLaunchAttribute attr[1];
-    const cudaLaunchConfig_t cfg = pdl_config(grid, dim3(tma::NT), tma::SMEM, s, attr);
-    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC>, p, m, first ? 1 : 0);
 }
 
 cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_t s) {
@@ -87,15 +57,9 @@ cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_
 }
 
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
-                            bool first, cudaStream_t s) {
-    if (scheme == SCHEME_REF) {
-        if (vel && prec) return launch_tma_t<SCHEME_REF, true, true>(p, m, grid, first, s);
-        if (vel) return launch_tma_t<SCHEME_REF, true, false>(p, m, grid, first, s);
-        if (prec) return launch_tma_t<SCHEME_REF, false, true>(p, m, grid, first, s);
-        return launch_tma_t<SCHEME_REF, false, false>(p, m, grid, first, s);
-    }
-    if (vel) return launch_tma_t<SCHEME_KSPACE, true, false>(p, m, grid, first, s);
-    return launch_tma_t<SCHEME_KSPACE, false, false>(p, m, grid, first, s);
+                            int tw, bool first, cudaStream_t s) {
+    if (tw == 64) return launch_step_tma64(p, m, scheme, vel, prec, grid, first, s);
+    return launch_step_tma_w<128>(p, m, scheme, vel, prec, grid, first, s);
 }
 
 }  // namespace bt

@@ -46,6 +46,8 @@
 // CTA then records status bit 8, drains its copies (bounded) and returns
 // without storing its partial.
 #pragma once
+#include <cstdlib>
+
 #include "bt_step.cuh"
 
 namespace bt {
@@ -53,32 +55,46 @@ namespace bt {
 namespace tma {
 
 constexpr int QX = 4;               // voxels per thread along x
-constexpr int TW = TMA_TX;          // 128
-constexpr int TH = TMA_TY;          // 8
-constexpr int NT = 32 * TH;         // 256 threads, one warp per row
+constexpr int NT = 256;             // threads per CTA
+constexpr int NWARP = NT / 32;      // warps per CTA (arrivals on an empty barrier)
 constexpr int NSTAGE = 3;
-constexpr int SW = TW + 8;          // state tile width: x0-4 .. x0+TW+3
-constexpr int SH = TH + 2;          // state tile height: y0-1 .. y0+TH
-constexpr int OFF_STATE = 0;
-constexpr int SZ_STATE = 3 * SH * SW * 4;                   // 16320
-constexpr int OFF_U = 16384;
-constexpr int SZ_U = 3 * TH * TW * 4;                       // 12288: upwind cell velocities, 3 axes
-constexpr int OFF_CODE = OFF_U + SZ_U;                      // 28672
-constexpr int SZ_CODE = TH * TW;                            // 1024
-constexpr int STAGE = OFF_CODE + SZ_CODE;                   // 29696
-constexpr int OFF_AUX = NSTAGE * STAGE;                     // tables, barriers, reduction
-// aux layout (bytes from OFF_AUX)
-constexpr int TAB_ROW = 12;                  // floats per code-table row: 48 B, so 8 distinct rows hit 8 bank groups
-constexpr int AUX_TAB = 0;                   // 128 rows: 6 face weights, dt/T1, dt/T2, 4 unused
-constexpr int AUX_EY = AUX_TAB + 128 * TAB_ROW * 4;  // 6144: exp(-i k_y y), TH float2
-constexpr int AUX_BARS = AUX_EY + 64;        // full[NSTAGE], empty[NSTAGE]
-constexpr int AUX_FLAGS = AUX_BARS + 64;
-constexpr int AUX_RED = AUX_FLAGS + 128;     // 8 warps x 3 doubles
-constexpr int AUX_EX = AUX_RED + 256;        // exp(-i k_x x), TW float2
-constexpr int AUX_EZ = AUX_EX + 8 * TW;      // exp(-i k_z z), up to ZCHUNK_MAX float2
-constexpr int SMEM = OFF_AUX + AUX_EZ + 8 * ZCHUNK_MAX + 128;  // + 128 for the base alignment
-static_assert(OFF_U % 128 == 0 && OFF_CODE % 128 == 0, "align");
-static_assert(STAGE % 128 == 0, "align");
+constexpr int TAB_ROW = 12;         // floats per code-table row: 48 B, so 8 distinct rows hit 8 bank groups
+
+// Tile geometry and shared-memory layout of the fast path for a tile TW
+// voxels wide: 128 (one 32-lane warp per row, 8 rows) or 64 (16 lanes per
+// row, two rows per warp, 16 rows) for narrow grids, where a 128-wide tile
+// would leave many lanes idle. Every thread holds 4 voxels along x.
+template <int TW_>
+struct Tile {
+    static_assert(TW_ == 128 || TW_ == 64, "tile width");
+    static constexpr int TW = TW_;
+    static constexpr int RPW = 128 / TW;          // rows per warp
+    static constexpr int LW = 32 / RPW;           // lanes per row
+    static constexpr int TH = NWARP * RPW;        // rows per tile
+    static constexpr int SW = TW + 8;             // state tile width: x0-4 .. x0+TW+3
+    static constexpr int SH = TH + 2;             // state tile height: y0-1 .. y0+TH
+    static constexpr int OFF_STATE = 0;
+    static constexpr int SZ_STATE = 3 * SH * SW * 4;
+    static constexpr int OFF_U = (SZ_STATE + 127) / 128 * 128;
+    static constexpr int SZ_U = 3 * TH * TW * 4;  // upwind cell velocities, 3 axes
+    static constexpr int OFF_CODE = OFF_U + SZ_U;
+    static constexpr int SZ_CODE = TH * TW;
+    static constexpr int STAGE = (OFF_CODE + SZ_CODE + 127) / 128 * 128;
+    static constexpr int OFF_AUX = NSTAGE * STAGE;  // tables, barriers, reduction
+    // aux layout (bytes from OFF_AUX)
+    static constexpr int AUX_TAB = 0;                     // 128 rows: 6 face weights, dt/T1, dt/T2, 4 unused
+    static constexpr int AUX_EY = AUX_TAB + 128 * TAB_ROW * 4;  // exp(-i k_y y), TH float2
+    static constexpr int AUX_BARS = AUX_EY + (8 * TH + 63) / 64 * 64;  // full[NSTAGE], empty[NSTAGE]
+    static constexpr int AUX_FLAGS = AUX_BARS + 64;
+    static constexpr int AUX_RED = AUX_FLAGS + 128;       // 8 warps x 3 doubles
+    static constexpr int AUX_EX = AUX_RED + 256;          // exp(-i k_x x), TW float2
+    static constexpr int AUX_EZ = AUX_EX + 8 * TW;        // exp(-i k_z z), up to ZCHUNK_MAX float2
+    static constexpr int SMEM = OFF_AUX + AUX_EZ + 8 * ZCHUNK_MAX + 128;  // + 128 for the base alignment
+    static_assert(OFF_U % 128 == 0 && OFF_CODE % 128 == 0 && STAGE % 128 == 0, "TMA destinations 128-aligned");
+    static_assert(TW + TH <= NT, "one phase-table entry per thread for x and y");
+};
+// the 128-wide tile keeps the layout the fast path was tuned with
+static_assert(Tile<128>::OFF_U == 16384 && Tile<128>::STAGE == 29696 && Tile<128>::AUX_BARS == 6208, "layout");
 constexpr uint32_t WAIT_LIMIT = 1u << 20;  // polls; a healthy copy lands in microseconds
 
 __device__ __forceinline__ uint32_t sa(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -134,7 +150,7 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
 
 // one thread per voxel (grid-stride): the fast path's gated cell velocities
 // u[axis][z][y][pitch]; face arrays as StepParams describes them
-__global__ void cell_velocity_kernel(const StepParams<float> P, float* __restrict__ u, long long comp) {
+static __global__ void cell_velocity_kernel(const StepParams<float> P, float* __restrict__ u, long long comp) {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const float h2[3] = {0.5f * P.hx, 0.5f * P.hy, 0.5f * P.hz};
     const long long n = (long long)nx * ny * nz;
@@ -154,10 +170,16 @@ __global__ void cell_velocity_kernel(const StepParams<float> P, float* __restric
     }
 }
 
-template <int SCHEME, bool VEL, bool PREC>
+template <int SCHEME, bool VEL, bool PREC, int TWV>
 __global__ void __launch_bounds__(tma::NT, 2)
     step_tma_kernel(const __grid_constant__ StepParams<float> P, const __grid_constant__ TmaMaps M, int first) {
     using namespace tma;
+    using Tl = Tile<TWV>;
+    constexpr int TW = Tl::TW, TH = Tl::TH, LW = Tl::LW, RPW = Tl::RPW, SW = Tl::SW, SH = Tl::SH;
+    constexpr int OFF_STATE = Tl::OFF_STATE, OFF_U = Tl::OFF_U, OFF_CODE = Tl::OFF_CODE, STAGE = Tl::STAGE;
+    constexpr int SZ_STATE = Tl::SZ_STATE, SZ_U = Tl::SZ_U, SZ_CODE = Tl::SZ_CODE, OFF_AUX = Tl::OFF_AUX;
+    constexpr int AUX_TAB = Tl::AUX_TAB, AUX_EY = Tl::AUX_EY, AUX_BARS = Tl::AUX_BARS, AUX_FLAGS = Tl::AUX_FLAGS;
+    constexpr int AUX_RED = Tl::AUX_RED, AUX_EX = Tl::AUX_EX, AUX_EZ = Tl::AUX_EZ;
     // TMA destinations must sit on 128-byte boundaries: align the dynamic
     // shared-memory base explicitly (the launch reserves 128 spare bytes)
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -173,6 +195,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, w = tid >> 5;
+    // this thread's row of the tile and lane within that row
+    const int row = w * RPW + lane / LW, xl = lane % LW;
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     // blockIdx.x walks the z-chunks of one tile. Odd chunks march downwards,
     // so the plane two neighbouring chunks share is read by both at the same
@@ -190,8 +214,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
     const int z0 = (int)((long long)zc * nz / P.zsplit);
     const int z1 = (int)((long long)(zc + 1) * nz / P.zsplit);
     const int d = (zc & 1) ? -1 : 1;
-    const int xb = x0 + QX * lane;  // first of this thread's 4 voxels
-    const int y = y0 + w;
+    const int xb = x0 + QX * xl;  // first of this thread's 4 voxels
+    const int y = y0 + row;
 
     uint32_t txbytes = SZ_STATE + SZ_CODE;
     if constexpr (VEL) txbytes += SZ_U;
@@ -214,7 +238,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
             mbar_init(&bars[s], 1);
-            mbar_init(&empties[s], TH);
+            mbar_init(&empties[s], NWARP);
         }
         fence_mbar_init();
         s_flags[0] = 0;
@@ -270,7 +294,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
     if constexpr (SCHEME == SCHEME_KSPACE) {
 #pragma unroll
         for (int i = 0; i < QX; ++i) {
-            const float2 e = s_ex[QX * lane + i];
+            const float2 e = s_ex[QX * xl + i];
             exr[i] = e.x;
             exi[i] = e.y;
         }
@@ -310,7 +334,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
         const float* st = reinterpret_cast<const float*>(smem + slot * STAGE + OFF_STATE);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float4 v = *reinterpret_cast<const float4*>(st + (c * SH + w + 1) * SW + 4 + QX * lane);
+            const float4 v = *reinterpret_cast<const float4*>(st + (c * SH + row + 1) * SW + 4 + QX * xl);
             dst[c][0] = v.x; dst[c][1] = v.y; dst[c][2] = v.z; dst[c][3] = v.w;
         }
     };
@@ -408,17 +432,17 @@ __global__ void __launch_bounds__(tma::NT, 2)
         float xm[3][QX], xp[3][QX], ym[3][QX], yp[3][QX];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float* row = st + (c * SH + w + 1) * SW + 4 + QX * lane;
-            const float4 a = *reinterpret_cast<const float4*>(row - SW);
-            const float4 b = *reinterpret_cast<const float4*>(row + SW);
+            const float* rp = st + (c * SH + row + 1) * SW + 4 + QX * xl;
+            const float4 a = *reinterpret_cast<const float4*>(rp - SW);
+            const float4 b = *reinterpret_cast<const float4*>(rp + SW);
             ym[c][0] = a.x; ym[c][1] = a.y; ym[c][2] = a.z; ym[c][3] = a.w;
             yp[c][0] = b.x; yp[c][1] = b.y; yp[c][2] = b.z; yp[c][3] = b.w;
             // x halo from the neighbouring lanes; only the tile edges read shared
             // memory (a stride-16-byte scalar load by every lane conflicts 4 ways)
-            float l = __shfl_up_sync(0xffffffffu, cur[c][QX - 1], 1);
-            float r = __shfl_down_sync(0xffffffffu, cur[c][0], 1);
-            if (lane == 0) l = row[-1];
-            if (lane == 31) r = row[QX];
+            float l = __shfl_up_sync(0xffffffffu, cur[c][QX - 1], 1, LW);
+            float r = __shfl_down_sync(0xffffffffu, cur[c][0], 1, LW);
+            if (xl == 0) l = rp[-1];
+            if (xl == LW - 1) r = rp[QX];
             xm[c][0] = l;
             xp[c][QX - 1] = r;
 #pragma unroll
@@ -443,10 +467,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
 #pragma unroll
             for (int i = 0; i < QX; ++i) ghost(yp[0][i], yp[1][i], yp[2][i], cur[0][i], cur[1][i], cur[2][i], 1, true);
         }
-        const uint32_t code4 = *reinterpret_cast<const uint32_t*>(base + OFF_CODE + w * TW + QX * lane);
+        const uint32_t code4 = *reinterpret_cast<const uint32_t*>(base + OFF_CODE + row * TW + QX * xl);
         float ux[QX] = {0.f, 0.f, 0.f, 0.f}, uy[QX] = {0.f, 0.f, 0.f, 0.f}, uz[QX] = {0.f, 0.f, 0.f, 0.f};
         if constexpr (VEL) {
-            const float* ur = reinterpret_cast<const float*>(base + OFF_U) + w * TW + QX * lane;
+            const float* ur = reinterpret_cast<const float*>(base + OFF_U) + row * TW + QX * xl;
             const float4 a = *reinterpret_cast<const float4*>(ur);
             const float4 b = *reinterpret_cast<const float4*>(ur + TH * TW);
             const float4 c = *reinterpret_cast<const float4*>(ur + 2 * TH * TW);
@@ -534,7 +558,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
         if constexpr (SCHEME == SCHEME_KSPACE) {
             // lab frame: multiply the row sum by exp(-i k_y y) exp(-i k_z z)
-            const float2 ey = s_ey[w], ez = s_ez[z - z0];
+            const float2 ey = s_ey[row], ez = s_ez[z - z0];
             const float er = ey.x * ez.x - ey.y * ez.y, ei = ey.x * ez.y + ey.y * ez.x;
             acc[0].add(er * sx_r - ei * sx_i);
             acc[1].add(er * sx_i + ei * sx_r);
@@ -596,6 +620,52 @@ abort:
                 if (mbar_try_wait(&bars[q % NSTAGE], (uint32_t)(q / NSTAGE) & 1u)) break;
     }
     __syncthreads();
+}
+
+// programmatic dependent launch: a kernel overlaps its step-independent
+// prologue with the previous launch's tail (BT_NO_PDL turns it off)
+static inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, int smem, cudaStream_t s,
+                                            cudaLaunchAttribute* attr) {
+    static const bool pdl = std::getenv("BT_NO_PDL") == nullptr;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cfg;
+}
+
+template <int SCHEME, bool VEL, bool PREC, int TWV>
+static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, bool first, cudaStream_t s) {
+    constexpr int smem = tma::Tile<TWV>::SMEM;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t cfg = pdl_config(grid, dim3(tma::NT), smem, s, attr);
+    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV>, p, m, first ? 1 : 0);
+}
+
+// the fast path's kernels of one tile width
+template <int TWV>
+static cudaError_t launch_step_tma_w(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec,
+                                     dim3 grid, bool first, cudaStream_t s) {
+    if (scheme == SCHEME_REF) {
+        if (vel && prec) return launch_tma_t<SCHEME_REF, true, true, TWV>(p, m, grid, first, s);
+        if (vel) return launch_tma_t<SCHEME_REF, true, false, TWV>(p, m, grid, first, s);
+        if (prec) return launch_tma_t<SCHEME_REF, false, true, TWV>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_REF, false, false, TWV>(p, m, grid, first, s);
+    }
+    if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV>(p, m, grid, first, s);
+    return launch_tma_t<SCHEME_KSPACE, false, false, TWV>(p, m, grid, first, s);
 }
 
 }  // namespace bt
