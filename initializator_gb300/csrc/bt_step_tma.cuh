@@ -1,7 +1,8 @@
 // FP32 fast path of the fused step (K1, TMA form) for sm_103a.
 //
 // Same update and M(t) as step_kernel (bt_step.cuh), for steps without pulses:
-//   * a CTA owns a 128 x 8 column tile and marches through a z-chunk (the
+//   * a CTA owns a 128 x 8 column tile (64 x 16 for grids a 128-wide tile
+//     would pad more: see Tile) and marches through a z-chunk (the
 //     column split into P.zsplit even chunks; odd chunks march downwards, so
 //     the plane two neighbouring chunks share is read by both at about the
 //     same moment and the second read hits L2);
@@ -13,7 +14,8 @@
 //     slot through the slot's "empty" mbarrier (one arrival per warp) and only
 //     the producing thread waits for it, so the warps of a CTA drift up to two
 //     planes apart instead of meeting at a CTA barrier every plane;
-//   * each thread computes 4 consecutive voxels along x: 128-bit shared
+//   * each thread computes 4 consecutive voxels along x (a warp holds one
+//     row of a 128-wide tile or two rows of a 64-wide one): 128-bit shared
 //     loads, 128-bit global stores; the voxel's own z-column (below / current
 //     / above) rolls through registers;
 //   * the stencil is evaluated as relaxation + sum over the six faces of
