@@ -129,7 +129,6 @@ cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int sc
 cudaError_t launch_step_tma64(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
                               bool first, cudaStream_t s);
 cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_t s);
-int tma_smem_bytes(int tw);
 // upwind cell velocities of the fast path from the face velocities, [axis][z][y][pitch]
 cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s);
 // tile of the fast path: tw = 128 or 64 voxels along x, tile_rows(tw) rows along y

@@ -41,7 +41,6 @@ cudaError_t launch_frame<float>(float* f[3], const uint8_t* code, int nx, int ny
     return cudaGetLastError();
 }
 
-int tma_smem_bytes(int tw) { return tw == 64 ? tma::Tile<64>::SMEM : tma::Tile<128>::SMEM; }
 
 cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s) {
     cell_velocity_kernel<<<1216, 256, 0, s>>>(p, u, comp);
