@@ -12,10 +12,14 @@
 //               cpp:2681-3146; M(t) printed AFTER each step into
 //               results_gpu.csv, final line into
 //               results_NMR/results_grad_<gx>_<gy>_<gz>.csv)
-// Both use the reference's explicit upwind update (ExplicitSimple,
-// cpp:3148-3282). The whole z-extent lives on one GPU, so MPI_size must be 1.
-// The arithmetic is FP64 (bit-identical fields) unless the environment sets
-// BT_PRECISION=f32, which selects the FP32 fast path.
+// Each steps with the update of its reference path: solve() with the explicit
+// upwind update (ExplicitSimple, cpp:3148-3282), solve_gpu() with the
+// predictor-corrector of the reference's kernels (NMR_predictor_upgrade /
+// NMR_corrector_upgrade, cu:637-967); BT_SCHEME=explicit makes solve_gpu()
+// use ExplicitSimple too. The whole z-extent lives on one GPU, so MPI_size
+// must be 1. The arithmetic is FP64 (bit-identical fields) unless the
+// environment sets BT_PRECISION=f32 (FP32 fields; ExplicitSimple steps then
+// take the FP32 fast path).
 #pragma once
 #include <string>
 #include <vector>
