@@ -208,6 +208,52 @@ def run_ragged(args, lr):
                          "frac": v_many * 25 / 1e9 / peak, "peak_kind": peak_kind, "bytes_per_voxel_step": 25}}
 
 
+C1_SHAPE = (64, 64, 64)
+C1_STEPS = 2000
+
+
+def run_c1(args, lr):
+    """C1, the compatibility configuration: 64^3 sphere pack (r 6, solid
+    0.35), no flow, no gradient, T1 2.5 s, T2 2.0 s, rho 10 um/s, the
+    reference's update (ExplicitSimple) in FP64 (bit-identical to the
+    reference's fields) and in FP32: 2000 time steps timed with CUDA events
+    after a warm-up of 64 (one step per launch of the generic FP64 kernel,
+    the fast path for FP32). Next to the reference's own CPU solve() at C1,
+    2.76e7 voxel-steps/s on one core."""
+    import torch
+
+    import initializator_gb300 as bt
+    from initializator_gb300 import geometry
+    mask = geometry.sphere_pack(C1_SHAPE, 6.0, 0.35, seed=SEED + 31)
+    kw = dict(dx=1e-6, dt=0.9 * (1e-6) ** 2 / (6 * 2.3e-9), d_pore=2.3e-9, t1=2.5, t2=2.0, rho1=1e-5, rho2=1e-5,
+              p_eq=1.0, main_field=(1.0, 0.0, 0.0), velocity=0, diffusion=1)
+    st0 = np.zeros((3,) + C1_SHAPE)
+    st0[1] = mask  # Mxy = 1, Mz = 0 in the pores
+    out = {}
+    for name, prec in (("f64", bt.BT_F64), ("f32", bt.BT_F32)):
+        with bt.Solver(bt.make_config(C1_SHAPE, precision=prec, **kw)) as s:
+            s.upload_geometry(mask)
+            s.set_state(st0)
+            s.run(64)
+            s.set_step(0)
+            s.set_state(st0)
+            stream = torch.cuda.ExternalStream(s.stream_ptr)
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            s.run_async(C1_STEPS)
+            ev1.record(stream)
+            s.synchronize()
+            ms = ev0.elapsed_time(ev1)
+            mt = s.read_mt(C1_STEPS)
+        out[name] = {"value": int(np.prod(C1_SHAPE)) * C1_STEPS / (ms / 1e3), "us_per_step": 1e3 * ms / C1_STEPS,
+                     "finite": bool(np.all(np.isfinite(mt)))}
+    return {"workload": "C1: 64^3 sphere pack r=6 solid 0.35, no flow, no gradient, reference update (ExplicitSimple)",
+            "unit": UNIT, "steps": C1_STEPS, **out,
+            "reference_cpu_1core": 2.76e7}
+
+
 C5_SHAPE = (768, 1024, 1024)  # C5: 1024 x 1024 x 768
 C5_STEPS = 500
 
@@ -490,6 +536,7 @@ def run_ours(args):
     qsweep = None if args.no_qsweep else run_qsweep(args, lr)
     ragged = None if args.no_ragged else run_ragged(args, lr)
     c5 = run_c5(args, lr) if args.c5 else None
+    c1 = run_c1(args, lr) if args.c1 else None
 
     out = None
     if r == 0:
@@ -513,6 +560,7 @@ def run_ours(args):
             "qsweep": qsweep,
             "ragged": ragged,
             "c5": c5,
+            "c1": c1,
         }
         print(json.dumps(out))
     if w > 1:
@@ -531,6 +579,7 @@ def main():
     ap.add_argument("--no-qsweep", action="store_true", help="skip the batched 32-gradient q-sweep (C3a) leg")
     ap.add_argument("--no-ragged", action="store_true", help="skip the 48-sample ragged batch (C3b) leg")
     ap.add_argument("--c5", action="store_true", help="add the 1024x1024x768 (C5, ~40 GB) leg")
+    ap.add_argument("--c1", action="store_true", help="add the 64^3 compatibility (C1, FP64 and FP32) leg")
     ap.add_argument("--zsplit", type=int, default=0, help="fixed z-chunking of the fast path (skips the autotuner)")
     ap.add_argument("--profile", action="store_true",
                     help="device-resident phase only (for ncu captures); prints no bench line")
