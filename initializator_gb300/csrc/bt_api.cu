@@ -439,6 +439,8 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
                 si.phase[2 * a][1] = std::sin(ang);
                 si.phase[2 * a + 1][0] = std::cos(ang);
                 si.phase[2 * a + 1][1] = -std::sin(ang);
+                si.phasef[a][0] = (float)si.phase[2 * a][0];
+                si.phasef[a][1] = (float)si.phase[2 * a][1];
             }
             if (c.scheme == BT_SCHEME_KSPACE && s < nsched)
                 for (int a = 0; a < 3; ++a) k[a] = k[a] + c.gamma * si.grad[a] * c.dt;

@@ -23,6 +23,7 @@ struct StepInfo {
     double grad[3];     // gradient during this step, T/m
     double knext[3];    // KSPACE: wave vector after this step (rad/m)
     double phase[6][2]; // KSPACE: face phase factor exp(-i k.(r_nb - r)) for -x,+x,-y,+y,-z,+z
+    float phasef[3][2]; // the -x, -y, -z factors rounded to FP32 (the fast path)
     int pulse_first;
     int pulse_count;
 };

@@ -275,16 +275,26 @@ __device__ __forceinline__ void cta_partial_acc(const StepParams<float>& P, unsi
             h = s + e;
             l = e - (h - s);
         }
-        if (lane == 0) red[warp * 3 + c] = (double)h + (double)l;
+        if (lane == 0) reinterpret_cast<float2*>(red)[warp * 3 + c] = make_float2(h, l);
     }
     __syncthreads();
+    // the warps' pairs added in warp order, still as float-float (the FP64
+    // pipe of this part is a small fraction of the FP32 one), stored in FP64
     if (tid == 0) {
-        double t[3] = {0.0, 0.0, 0.0};
-        for (int w = 0; w < nwarps; ++w)
+        const float2* pr = reinterpret_cast<const float2*>(red);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) t[c] += red[w * 3 + c];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) P.partials[3ull * ((unsigned long long)b * nb_per + local) + c] = t[c];
+        for (int c = 0; c < 3; ++c) {
+            float h = pr[c].x, l = pr[c].y;
+            for (int w = 1; w < nwarps; ++w) {
+                const float2 q = pr[w * 3 + c];
+                float s, e;
+                two_sum(h, q.x, s, e);
+                e += l + q.y;
+                h = s + e;
+                l = e - (h - s);
+            }
+            P.partials[3ull * ((unsigned long long)b * nb_per + local) + c] = (double)h + (double)l;
+        }
     }
 }
 

@@ -313,8 +313,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
     if constexpr (SCHEME == SCHEME_KSPACE) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            ph[a][0] = (float)si->phase[2 * a][0];
-            ph[a][1] = (float)si->phase[2 * a][1];
+            ph[a][0] = si->phasef[a][0];
+            ph[a][1] = si->phasef[a][1];
         }
     }
     // summation mask of this thread's 4 voxels (trimming box, inside the grid)
