@@ -382,19 +382,39 @@ def _cuda_tensor_from_ptr(ptr, n, dtype):
     return torch.as_tensor(w, device="cuda")
 
 
-def kspace_waveform_pgse(nsteps, dt, g_amp, delta, Delta, axis=(0.0, 0.0, 1.0)):
+def kspace_waveform_pgse(nsteps, dt, g_amp, delta, Delta, axis=(0.0, 0.0, 1.0), ramp=0.0):
     """Per-step gradient (T/m) of a PGSE sequence: lobes of length delta at
     [0, delta) and [Delta, Delta + delta), both positive (a 180 pulse at Delta/2
-    between them refocuses). Step i covers [i*dt, (i+1)*dt); its value is the
-    lobe's fraction of that interval."""
+    between them refocuses). With ramp > 0 each lobe is a trapezoid: a linear
+    rise over `ramp` seconds, the plateau at g_amp, a linear fall over the
+    last `ramp` seconds of the lobe (2 ramp <= delta). Step i covers
+    [i*dt, (i+1)*dt); its value is the lobe's exact average over that interval,
+    so k = gamma * sum(G dt) is exact at every step boundary."""
+    if ramp < 0.0 or 2.0 * ramp > delta:
+        raise ValueError("ramp must be in [0, delta / 2]")
     t0 = np.arange(nsteps) * dt
     t1 = t0 + dt
-
-    def overlap(a, b):
-        return np.clip(np.minimum(t1, b) - np.maximum(t0, a), 0.0, None) / dt
-
-    f = overlap(0.0, delta) + overlap(Delta, Delta + delta)
     ax = np.asarray(axis, dtype=np.float64)
+    if ramp == 0.0:
+        # rectangular lobes: each step's overlap with them, directly
+        def overlap(a, b):
+            return np.clip(np.minimum(t1, b) - np.maximum(t0, a), 0.0, None) / dt
+
+        f = overlap(0.0, delta) + overlap(Delta, Delta + delta)
+        return (f[:, None] * g_amp) * ax[None, :]
+
+    def area(start, t):
+        # integral of one unit-height lobe from its start to t
+        tau = np.clip(t - start, 0.0, delta)
+        e, p = ramp, delta - 2.0 * ramp
+        up = np.minimum(tau, e)
+        a = up * up / (2.0 * e)                               # the rise
+        a += np.clip(tau - e, 0.0, p)                         # the plateau
+        dn = np.clip(tau - e - p, 0.0, e)
+        a += dn - dn * dn / (2.0 * e)                         # the fall
+        return a
+
+    f = (area(0.0, t1) - area(0.0, t0) + area(Delta, t1) - area(Delta, t0)) / dt
     return (f[:, None] * g_amp) * ax[None, :]
 
 
