@@ -241,13 +241,16 @@ def test_conservation_256(btlib):
     assert abs(mt[-1, 0] / mask.sum() - 1.0) < 1e-5
 
 
-@pytest.mark.parametrize("shape", [(33, 9, 65), (8, 16, 130), (5, 17, 257), (70, 3, 4)])
+@pytest.mark.parametrize("shape,flow", [((33, 9, 65), True), ((8, 16, 130), True), ((5, 17, 257), True),
+                                        ((70, 3, 4), True), ((12, 20, 40), False), ((9, 40, 120), False)])
 @pytest.mark.parametrize("scheme", [0, 1])
-def test_tma_path_matches_generic(shape, scheme, btlib, monkeypatch):
+def test_tma_path_matches_generic(shape, flow, scheme, btlib, monkeypatch):
     """The FP32 TMA fast path (pulse-free steps) against the generic FP32 kernel:
-    same update, different FP32 operation order -> fields within 1e-5."""
+    same update, different FP32 operation order -> fields within 1e-5. Widths
+    65 and 120 take 128-wide tiles, 4, 40, 130 and 257 64-wide ones (the width
+    that pads x less); with and without flow."""
     import initializator_gb300 as bt
-    mask, vel, st0, kw = _random_case(shape, seed=11 + sum(shape))
+    mask, vel, st0, kw = _random_case(shape, seed=11 + sum(shape), flow=flow)
     if scheme == bt.BT_SCHEME_KSPACE:
         kw.update(main_field=(0, 0, 1), vector_mult=0, gamma=bt.GAMMA_PROTON)
         wave = bt.kspace_waveform_pgse(80, kw["dt"], 0.05, 8 * kw["dt"], 40 * kw["dt"], axis=(0.2, 0.5, 1.0))
