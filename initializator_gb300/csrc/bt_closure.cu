@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(128) umma_selftest_kernel(const __nv_bfloat16*
     __shared__ __align__(1024) unsigned char sm[4096 + 512 + 64];
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 4096 + 512);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 4096 + 512 + 16);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, warp = tid >> 5;
     // canonical K-major no-swizzle: chunk kc (8 K elements) of row r at kc*2048 + r*16
     {
         const uint4* src = reinterpret_cast<const uint4*>(A + tid * 16);

@@ -135,7 +135,7 @@ __device__ __forceinline__ void finish_step_red(const StepParams<T>& P, long lon
                                                 unsigned nb_per, double* red, int* flag) {
     const int nthreads = blockDim.x * blockDim.y;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-    const int lane = tid & 31, warp = tid >> 5, nwarps = nthreads / 32;
+    const int nwarps = nthreads / 32;
     __syncthreads();
     const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
     if (tid == 0) {
