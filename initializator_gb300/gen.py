@@ -18,6 +18,9 @@ Presets follow the synthetic workloads (grid, geometry, flow, fluid):
        (tens of GB of text in the reference's formats; --device cuda generates it faster)
 Every Nmr_data.dat parameter can be set with --set name=value (the field
 names of datfiles.NmrData); n_velocity follows --flow unless set explicitly.
+--surfrel-water R1 R2 (and --surfrel-oil) writes SurfRel{1,2}<fluid>{X,Y,Z}.dat
+face relaxivities (m/s) and switches nSurfRel<fluid> on; --surfrel-spread f
+scales each face by a seeded factor in [1 - f, 1 + f].
 """
 from __future__ import annotations
 
@@ -97,6 +100,12 @@ def main(argv=None):
     ap.add_argument("--n1", type=float, help="uniform phase-1 concentration for two components (n1_init.dat)")
     ap.add_argument("--n1-random", type=float, nargs=2, metavar=("LOW", "HIGH"),
                     help="seeded uniform phase-1 concentration in [LOW, HIGH) (n1_init.dat)")
+    ap.add_argument("--surfrel-water", type=float, nargs=2, metavar=("R1", "R2"),
+                    help="face relaxivities of water (SurfRel1WaterX.dat ... SurfRel2WaterZ.dat), m/s")
+    ap.add_argument("--surfrel-oil", type=float, nargs=2, metavar=("R1", "R2"),
+                    help="face relaxivities of oil (SurfRel1OilX.dat ... SurfRel2OilZ.dat), m/s")
+    ap.add_argument("--surfrel-spread", type=float, default=0.0,
+                    help="seeded relative spread of the face relaxivities")
     ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE",
                     help="an Nmr_data.dat parameter (datfiles.NmrData field name)")
     ap.add_argument("--device", default="cpu", help="torch device for the generators")
@@ -118,6 +127,10 @@ def main(argv=None):
     mask, vel = build_case(spec, seed=args.seed, device=args.device)
     data_kw = dict(spec["data"])
     data_kw["n_velocity"] = 1 if vel is not None else 0
+    if args.surfrel_water is not None:
+        data_kw["n_surf_rel_water"] = 1
+    if args.surfrel_oil is not None:
+        data_kw["n_surf_rel_oil"] = 1
     data_kw.update(_parse_set(args.set))
     data = datfiles.NmrData(**data_kw)
     if data.n_velocity == 1 and vel is None:
@@ -130,13 +143,28 @@ def main(argv=None):
         n1 = np.random.default_rng(args.seed + 2).uniform(lo, hi, mask.shape).astype(np.float32)
     if data.n_components == 2 and n1 is None:
         ap.error("n_components=2 needs --n1 or --n1-random")
+    if args.surfrel_spread < 0.0 or args.surfrel_spread >= 1.0:
+        ap.error("--surfrel-spread must be in [0, 1)")
+    surfrel = {}
+    rng = np.random.default_rng(args.seed + 3)
+    nz_, ny_, nx_ = mask.shape
+    faces = ((nz_, ny_, nx_ + 1), (nz_, ny_ + 1, nx_), (nz_ + 1, ny_, nx_))
+    for fluid, vals, flag in (("Water", args.surfrel_water, data.n_surf_rel_water),
+                              ("Oil", args.surfrel_oil, data.n_surf_rel_oil)):
+        if flag == 1 and vals is None:
+            ap.error(f"nSurfRel{fluid} = 1 needs --surfrel-{fluid.lower()}")
+        if vals is None:
+            continue
+        for n, r in zip("12", vals):
+            s = args.surfrel_spread
+            surfrel[n + fluid] = tuple(r * (1.0 + rng.uniform(-s, s, f)) if s > 0 else np.full(f, r) for f in faces)
 
     datfiles.write_case(args.out, data, mask, vel=None if data.n_velocity != 1 else vel, grads=tuple(args.grad),
-                        n1=n1)
+                        surfrel=surfrel, n1=n1)
     nx, ny, nz = spec["shape"]
     summary = {"dir": os.path.join(args.out, "data"), "shape": [nx, ny, nz], "geometry": spec["geometry"],
                "seed": args.seed, "porosity": float(mask.mean()), "velocity": data.n_velocity == 1,
-               "two_components": data.n_components == 2}
+               "two_components": data.n_components == 2, "surfrel": sorted(surfrel)}
     print(json.dumps(summary))
     return 0
 

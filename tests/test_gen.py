@@ -57,11 +57,31 @@ def test_presets_and_two_components(tmp_path):
     assert n1.shape == (5, 6, 8) and np.all(n1 == np.float32(0.7))
 
 
+def test_surfrel_files(tmp_path):
+    """Face relaxivity files for water: constant values with a seeded spread,
+    read back in the package's face layout; nSurfRelWater switched on."""
+    from initializator_gb300 import datfiles
+    d = str(tmp_path / "s")
+    out = run_gen(d, "--shape", "6", "5", "4", "--geometry", "open", "--surfrel-water", "1e-5", "2e-5",
+                  "--surfrel-spread", "0.2", "--seed", "9")
+    assert out.returncode == 0, out.stderr
+    assert json.loads(out.stdout.strip().splitlines()[-1])["surfrel"] == ["1Water", "2Water"]
+    data_dir = os.path.join(d, "data")
+    data = datfiles.read_data(os.path.join(data_dir, "Nmr_data.dat"))
+    assert data.n_surf_rel_water == 1 and data.n_surf_rel_oil == 0
+    fx, fy, fz = datfiles.read_surfrel(data_dir, "2Water", 6, 5, 4)
+    assert fx.shape == (4, 5, 7) and fy.shape == (4, 6, 6) and fz.shape == (5, 5, 6)
+    for a in (fx, fy, fz):
+        assert np.all(a >= 2e-5 * 0.8) and np.all(a <= 2e-5 * 1.2) and a.std() > 0
+    assert not os.path.exists(os.path.join(data_dir, "SurfRel1OilX.dat"))
+
+
 @pytest.mark.parametrize("args", [
     ["--shape", "4", "4", "4"],                                       # no geometry
     ["--shape", "4", "4", "4", "--geometry", "spheres"],              # no radius / solid fraction
     ["--shape", "4", "4", "4", "--geometry", "open", "--set", "bogus=1"],
     ["--shape", "4", "4", "4", "--geometry", "open", "--set", "n_components=2"],  # no n1
+    ["--shape", "4", "4", "4", "--geometry", "open", "--set", "n_surf_rel_oil=1"],  # no oil relaxivities
 ])
 def test_rejects_incomplete_cases(tmp_path, args):
     out = run_gen(str(tmp_path / "x"), *args)
