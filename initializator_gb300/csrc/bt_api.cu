@@ -555,10 +555,20 @@ void convert(D* dst, const S* src, size_t n) {
         part(0);
         return;
     }
+    // a thread that cannot be started (a process limit) leaves its slice to
+    // the calling thread: no exception crosses the C ABI
     std::vector<std::thread> ts;
     ts.reserve(nt - 1);
-    for (unsigned t = 1; t < nt; ++t) ts.emplace_back(part, t);
+    std::vector<unsigned> left;
+    for (unsigned t = 1; t < nt; ++t) {
+        try {
+            ts.emplace_back(part, t);
+        } catch (...) {
+            left.push_back(t);
+        }
+    }
     part(0);
+    for (unsigned t : left) part(t);
     for (auto& t : ts) t.join();
 }
 
