@@ -576,24 +576,24 @@ def rollout(cc: CoarseCase, closure: Closure = None, check_every=0, check_tol=2e
         if fine is not None:
             mt[n] = fine.run(4)[-1]
             continue
-        judge = None
+        check = None
         if closure is not None and check_every and n > 0 and n % check_every == 0:
-            judge = case.solver(state=False)
-            judge.set_step(4 * n)
-            _write_views(judge, cc.prolong(crs.field_views(), 4 * n))
-            before = judge.measure()
-            after_f = judge.run(4)[-1]
+            check = case.solver(state=False)
+            check.set_step(4 * n)
+            _write_views(check, cc.prolong(crs.field_views(), 4 * n))
+            before = check.measure()
+            after_f = check.run(4)[-1]
         crs.run(1)
         if closure is not None:
             closure.apply(crs, cc, n)
         mt[n] = cc.mt(crs, n + 1)
-        if judge is not None:
+        if check is not None:
             d = np.abs((mt[n] - before) - (after_f - before)).max()
             if d > check_tol * max(np.abs(before).max(), 1e-300):
-                fell_back, fine = n, judge
+                fell_back, fine = n, check
                 mt[n] = after_f
                 continue
-            judge.close()
+            check.close()
     crs.close()
     if fine is not None:
         fine.close()
