@@ -60,6 +60,26 @@ extern "C" {
 #define BT_SCHEME_KSPACE 1
 #define BT_SCHEME_MACCORMACK 2
 
+/* Ghost layer of a domain-face pair (bt_config.boundary, per axis x, y, z), as
+ * the reference's GPU path leaves it after BoundaryConditionsForVectorField_gpu
+ * (src/NmrRelaxationSolveKernels.cu:1321-1396) for nBoundary1..6 of
+ * Nmr_data.dat (x: 1 and 3, y: 2 and 4, z: 5 and 6):
+ *   BT_BC_COPY      both faces 1: the edge cell (BC_ZeroDer_*, cu:969-1000; the
+ *                   CPU path's only kind, cpp:1664-1754)
+ *   BT_BC_PERIODIC  both faces 3: the far edge cell (BC_Inf_*, cu:1002-1033)
+ *   BT_BC_ZERO      x with a face 2: zero (BC_Advanced_XM/XP with 0, cu:1035-1053);
+ *                   any other pair, which that routine leaves alone: its ghost
+ *                   cells are never written and hold zero
+ * In every kind the first step of a run that starts at step 0 reads the
+ * field's ghosts as copies of the edge cells, as the reference's arrays hold
+ * them before its first step (FillInMagnetization + InitializeGpu); the
+ * MacCormack predictor's ghosts follow the kind from the first step on. The
+ * face diffusivity of a domain face pairs the edge cell with itself in every
+ * kind (BoundaryConditionsForDiffusion copies). */
+#define BT_BC_COPY 0
+#define BT_BC_PERIODIC 1
+#define BT_BC_ZERO 2
+
 typedef struct bt_config {
     int nx, ny, nz;        /* interior cells (Nmr_start.dat: ik, jk, kk) */
     int precision;         /* BT_F32 / BT_F64 */
@@ -78,6 +98,8 @@ typedef struct bt_config {
     double t1, t2;         /* bulk relaxation times of the fluid, s */
     double rho1, rho2;     /* surface relaxivities, m/s (rate rho/d per solid face) */
     double p_eq;           /* equilibriumMagnetization (cpp:810) */
+    int boundary[3];       /* BT_BC_* per axis x, y, z (0 = copy, the default) */
+    int reserved;
 } bt_config;
 
 /* An instantaneous pulse applied right after the update of step `step`
@@ -200,6 +222,16 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit);
  * (or bt_autotune) sets it back for running alone. */
 int bt_set_tma_split(bt_handle* h, int zsplit);
 
+/* Failure injection for tests (no reference counterpart): the FP32 fast
+ * path's plane-ring waits (mbarrier polls for a plane's TMA copy, and the
+ * producer's wait for a free ring slot) give up after `polls` polls, 0 = at
+ * once, so that a test sees the bounded-wait path run: every CTA that gives
+ * up raises its failure flag, waits (with the full bound) for its own copies
+ * in flight and exits, and the run returns BT_E_TIMEOUT; the handle stays
+ * usable (bt_set_state, then bt_run). polls < 0 restores the default bound
+ * (2^20 polls, far beyond what a healthy copy needs). */
+int bt_set_wait_polls(bt_handle* h, long long polls);
+
 /* Device pointers of the current field of batch member `member` (no
  * reference counterpart: the learned closure corrects the field in place).
  * Layout [nz][ny][pitch] in the handle's precision; for the KSPACE scheme the
@@ -227,15 +259,18 @@ long long bt_launch_count(const bt_handle* h);
  * cfg->precision: mask; face velocities (NULL when cfg->velocity == 0); the
  * field in (mx_in, my_in, mz_in) and out (must not alias the inputs); sums
  * receives the three M(t) sums of the new field (3 doubles, device memory).
- * The static gradient cfg->grad applies; no pulses. Asynchronous on
- * `stream` (a cudaStream_t, NULL = legacy default stream).
+ * The static gradient cfg->grad applies; no pulses. One field per call:
+ * cfg->batch must be 0 or 1, cfg->velocity 0 or 1 and cfg->boundary all
+ * BT_BC_COPY (BT_E_ARG otherwise).
+ * Asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream).
  * The scratch (run control, schedule record, per-CTA partial sums, geometry
  * code) is one file-scope __device__ array shared by every call on a device
  * and keeping the last call's contents; each call re-initialises it, so calls
  * ordered on one stream are independent, but calls that overlap on the GPU
- * race and must not be issued. The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) and should come before any
- * stream capture. Grids above BT_NOALLOC_MAX_VOXELS voxels or
+ * race and must not be issued. The first call on a device (and the first
+ * after its context was reset) looks up the array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture. Grids
+ * above BT_NOALLOC_MAX_VOXELS voxels or
  * BT_NOALLOC_MAX_BLOCKS blocks return BT_E_SIZE (with a message on stderr).
  * A NaN/Inf field shows as non-finite sums (no watchdog status here). */
 int bt_step_noalloc(const bt_config* cfg, const uint8_t* mask, const void* vx, const void* vy, const void* vz,

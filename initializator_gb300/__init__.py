@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(PKG, "_build", "libbt.so")
 BT_OK = 0
 BT_F32, BT_F64 = 0, 1
 BT_SCHEME_REFERENCE, BT_SCHEME_KSPACE, BT_SCHEME_MACCORMACK = 0, 1, 2
+BT_BC_COPY, BT_BC_PERIODIC, BT_BC_ZERO = 0, 1, 2
 GAMMA_REFERENCE = 4.78941714e7   # the reference's hard-coded g (cpp:807)
 GAMMA_PROTON = 2.675e8            # rad/s/T
 
@@ -41,6 +42,7 @@ class Config(ctypes.Structure):
         ("main_field", ctypes.c_double * 3), ("gamma", ctypes.c_double), ("grad", ctypes.c_double * 3),
         ("d_pore", ctypes.c_double), ("t1", ctypes.c_double), ("t2", ctypes.c_double),
         ("rho1", ctypes.c_double), ("rho2", ctypes.c_double), ("p_eq", ctypes.c_double),
+        ("boundary", ctypes.c_int * 3), ("reserved", ctypes.c_int),
     ]
 
 
@@ -71,7 +73,7 @@ EXPORTS = [
     "bt_read_mt_phases", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
     "bt_version", "bt_autotune", "bt_set_tma_split", "bt_step_noalloc",
     "bt_conv3d_margin", "bt_conv3d", "bt_conv3d_weight_grad", "bt_conv3d_wgrad_scratch", "bt_conv3d_pack_weights",
-    "bt_adamw", "bt_umma_selftest", "bt_field_device",
+    "bt_adamw", "bt_umma_selftest", "bt_field_device", "bt_set_wait_polls",
 ]
 
 _lib = None
@@ -114,6 +116,7 @@ def lib():
         "bt_version": ([], ctypes.c_char_p),
         "bt_autotune": ([vp, i, ctypes.POINTER(ctypes.c_int)], i),
         "bt_set_tma_split": ([vp, i], i),
+        "bt_set_wait_polls": ([vp, ll], i),
         "bt_step_noalloc": ([ctypes.POINTER(Config), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
         "bt_conv3d_margin": ([i, i], ll),
         "bt_conv3d": ([ctypes.POINTER(Conv3dArgs), vp], i),
@@ -141,7 +144,7 @@ def _dp(a):
 def make_config(shape, *, dx, dy=None, dz=None, dt, precision=BT_F32, scheme=BT_SCHEME_REFERENCE,
                 main_field=(1.0, 0.0, 0.0), gamma=GAMMA_REFERENCE, grad=(0.0, 0.0, 0.0), d_pore=2.3e-9,
                 t1=2.5, t2=2.0, rho1=0.0, rho2=0.0, p_eq=1.0, vector_mult=0, velocity=0, diffusion=1,
-                buffer=(0, 0, 0), batch=1) -> Config:
+                buffer=(0, 0, 0), batch=1, boundary=(0, 0, 0)) -> Config:
     nz, ny, nx = shape
     c = Config()
     c.batch = batch
@@ -157,7 +160,16 @@ def make_config(shape, *, dx, dy=None, dz=None, dt, precision=BT_F32, scheme=BT_
     c.gamma = gamma
     c.grad[:] = list(grad)
     c.d_pore, c.t1, c.t2, c.rho1, c.rho2, c.p_eq = d_pore, t1, t2, rho1, rho2, p_eq
+    c.boundary[:] = list(boundary)
     return c
+
+
+def boundary_from_nb(nb):
+    """bt_config.boundary for nBoundary1..6 of Nmr_data.dat: per axis (x: 1 and
+    3, y: 2 and 4, z: 5 and 6) copy when both faces are 1, periodic when both
+    are 3, zero otherwise (the reference's GPU path, cu:1321-1396)."""
+    pairs = [(nb[0], nb[2]), (nb[1], nb[3]), (nb[4], nb[5])]
+    return tuple(BT_BC_COPY if p == (1, 1) else BT_BC_PERIODIC if p == (3, 3) else BT_BC_ZERO for p in pairs)
 
 
 def sequence_schedule(n_sequence, nsteps, *, dt, time1=0.0, time2=0.0, direction=(1.0, 0.0, 0.0),
@@ -333,6 +345,11 @@ class Solver:
         """The FP32 fast path's z-chunks per column (0: the default for running
         alone; run_many sets them for sharing the GPU)."""
         self._check(self._l.bt_set_tma_split(self._h, int(zsplit)), "set_tma_split")
+
+    def set_wait_polls(self, polls=-1):
+        """Failure injection: the fast path's plane-ring waits give up after
+        `polls` polls (0 = at once); -1 restores the default bound."""
+        self._check(self._l.bt_set_wait_polls(self._h, int(polls)), "set_wait_polls")
 
     def field_views(self, member=0):
         """torch views (3 x [nz][ny][nx], strided by the pitch) of the current

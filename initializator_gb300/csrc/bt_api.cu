@@ -91,6 +91,7 @@ struct bt_handle {
     double* mt6_d = nullptr;
     long long mt6_cap = 0;
     std::vector<uint8_t> mask_h;  // host copy of the pore mask (two-component sums)
+    uint32_t wait_polls = bt::RING_WAIT_POLLS;  // fast path's plane-ring wait bound
 };
 
 namespace {
@@ -195,6 +196,7 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
             P.dtt2[f] = (T)(dTime * tau2);
         }
         P.diffusion = c.diffusion ? 1 : 0;
+        for (int a = 0; a < 3; ++a) P.bc[a] = c.boundary[a];
         P.box[0] = c.buffer[0]; P.box[1] = c.nx - c.buffer[0];
         P.box[2] = c.buffer[1]; P.box[3] = c.ny - c.buffer[1];
         P.box[4] = c.buffer[2]; P.box[5] = c.nz - c.buffer[2];
@@ -211,6 +213,7 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
         P.fstride = (long long)h->comp;
         P.fdtt = h->fields_d ? static_cast<const T*>(h->fields_d) : nullptr;
         P.fw = h->fields_d ? static_cast<const T*>(h->fields_d) + 2 * h->comp : nullptr;
+        P.wait_polls = h->wait_polls;
     }
 }
 
@@ -324,6 +327,13 @@ int default_tma_split(const bt_handle* h) {
     zs = std::min<long long>(zs, std::max(1, c.nz / 8));
     if (const char* e = std::getenv("BT_TMA_ZSPLIT")) zs = std::max(1, std::atoi(e));
     return (int)std::max<long long>(1, zs);
+}
+
+// the FP32 fast path serves this configuration (non-copy faces: KSPACE only)
+bool fast_path_config(const bt_config& c) {
+    if (c.precision != BT_F32 || c.scheme == BT_SCHEME_MACCORMACK || std::getenv("BT_NO_TMA")) return false;
+    return c.scheme == BT_SCHEME_KSPACE ||
+           (c.boundary[0] == BT_BC_COPY && c.boundary[1] == BT_BC_COPY && c.boundary[2] == BT_BC_COPY);
 }
 
 bool step_has_pulse(const bt_handle* h, long long s) {
@@ -441,6 +451,14 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
                 si.phase[2 * a + 1][1] = -std::sin(ang);
                 si.phasef[a][0] = (float)si.phase[2 * a][0];
                 si.phasef[a][1] = (float)si.phase[2 * a][1];
+                // periodic faces: exp(-i k_a n_a d_a), the far edge cell's
+                // k-frame value moved across the period
+                const int n3[3] = {c.nx, c.ny, c.nz};
+                const double wa = k[a] * ((double)n3[a] * d3[a]);
+                si.wrap[a][0] = std::cos(wa);
+                si.wrap[a][1] = -std::sin(wa);
+                si.wrapf[a][0] = (float)si.wrap[a][0];
+                si.wrapf[a][1] = (float)si.wrap[a][1];
             }
             if (c.scheme == BT_SCHEME_KSPACE && s < nsched)
                 for (int a = 0; a < 3; ++a) k[a] = k[a] + c.gamma * si.grad[a] * c.dt;
@@ -638,6 +656,9 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     if (!(cfg->dt > 0) || !(cfg->dx > 0) || !(cfg->dy > 0) || !(cfg->dz > 0)) return BT_E_ARG;
     for (int a = 0; a < 3; ++a)
         if (cfg->buffer[a] < 0 || 2 * cfg->buffer[a] > (a == 0 ? cfg->nx : a == 1 ? cfg->ny : cfg->nz)) return BT_E_ARG;
+    for (int a = 0; a < 3; ++a)
+        if (cfg->boundary[a] != BT_BC_COPY && cfg->boundary[a] != BT_BC_PERIODIC && cfg->boundary[a] != BT_BC_ZERO)
+            return BT_E_ARG;
     const long long nvox = (long long)cfg->nx * cfg->ny * cfg->nz;
     if (nvox > (1LL << 40) || cfg->nx > (1 << 28) || cfg->ny > (1 << 28)) return BT_E_ARG;
     bt_handle* h = new bt_handle();
@@ -688,7 +709,7 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
             if (cudaMalloc(&h->vel[a], h->esz * n3[a]) != cudaSuccess) return bail(BT_E_NOMEM);
             cudaMemset(h->vel[a], 0, h->esz * n3[a]);
         }
-        if (cfg->precision == BT_F32 && cfg->scheme != BT_SCHEME_MACCORMACK && !std::getenv("BT_NO_TMA")) {
+        if (fast_path_config(*cfg)) {
             if (cudaMalloc(&h->ucell, sizeof(float) * 3 * h->comp) != cudaSuccess) return bail(BT_E_NOMEM);
             cudaMemset(h->ucell, 0, sizeof(float) * 3 * h->comp);
         }
@@ -711,7 +732,7 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
     if (rc) return bail(rc);
     rc = build_schedule(h, nullptr, 0, nullptr, 0);
     if (rc) return bail(rc);
-    if (cfg->precision == BT_F32 && cfg->scheme != BT_SCHEME_MACCORMACK && !std::getenv("BT_NO_TMA")) {
+    if (fast_path_config(*cfg)) {
         // 64-wide tiles where they pad x less than 128-wide ones (narrow or
         // odd widths); BT_TMA_TW = 64 / 128 forces one
         h->ttx = ((cfg->nx + 63) / 64) * 64 < ((cfg->nx + 127) / 128) * 128 ? 64 : 128;
@@ -792,9 +813,7 @@ int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, cons
         }
     }
     h->geometry = true;
-    if (h->cfg.precision == BT_F32 && h->cfg.scheme != BT_SCHEME_MACCORMACK && h->tgrid.y > 0 &&
-        !std::getenv("BT_NO_TMA"))
-        h->use_tma = build_maps(h);
+    if (fast_path_config(h->cfg) && h->tgrid.y > 0) h->use_tma = build_maps(h);
     refresh_params(h);
     return BT_OK;
 }
@@ -1174,6 +1193,14 @@ int bt_field_device(bt_handle* h, int member, void** mx, void** my, void** mz, i
     *my = (char*)h->state[h->cur][1] + off;
     *mz = (char*)h->state[h->cur][2] + off;
     *pitch = h->pitch;
+    return BT_OK;
+}
+
+int bt_set_wait_polls(bt_handle* h, long long polls) {
+    if (!h) return BT_E_ARG;
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->wait_polls = polls < 0 ? bt::RING_WAIT_POLLS : (uint32_t)std::min<long long>(polls, 0xffffffffLL);
+    refresh_params(h);  // the parameters are baked into the captured graphs
     return BT_OK;
 }
 

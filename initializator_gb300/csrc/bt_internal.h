@@ -11,6 +11,9 @@ constexpr int TX = 32;
 constexpr int TY = 8;
 constexpr int NTHREADS = TX * TY;
 constexpr int MAX_PULSES_PER_STEP = 8;
+// default bound (polls) of the FP32 fast path's plane-ring waits; a healthy
+// copy lands in microseconds
+constexpr uint32_t RING_WAIT_POLLS = 1u << 20;
 
 // Bits of the per-voxel geometry code (one byte per voxel): bit f (0..5) is
 // set when the face neighbour f = -x,+x,-y,+y,-z,+z is an in-domain solid
@@ -18,12 +21,22 @@ constexpr int MAX_PULSES_PER_STEP = 8;
 // relaxation-rate tables (surface relaxation rho/d per solid face).
 constexpr uint8_t CODE_PORE = 64;
 
+// ghost layer kinds of a domain-face pair (bt_config.boundary)
+constexpr int BC_COPY = 0;
+constexpr int BC_PERIODIC = 1;
+constexpr int BC_ZERO = 2;
+
 // Per-step schedule record (one per step, read uniformly by every CTA).
 struct StepInfo {
     double grad[3];     // gradient during this step, T/m
     double knext[3];    // KSPACE: wave vector after this step (rad/m)
     double phase[6][2]; // KSPACE: face phase factor exp(-i k.(r_nb - r)) for -x,+x,-y,+y,-z,+z
     float phasef[3][2]; // the -x, -y, -z factors rounded to FP32 (the fast path)
+    // KSPACE with periodic faces: exp(-i k_a n_a d_a) per axis; the k-frame
+    // value of a lower face's ghost is the far edge cell's times this, an
+    // upper face's ghost the far edge cell's times its conjugate
+    double wrap[3][2];
+    float wrapf[3][2];
     int pulse_first;
     int pulse_count;
 };
@@ -80,6 +93,7 @@ struct StepParams {
     T dpp, dps;                 // harmonic-mean face diffusivity pore-pore / pore-solid
     T dtt1[64], dtt2[64];       // dTime * (1/T1), dTime * (1/T2) per face code
     int diffusion;
+    int bc[3];                  // ghost layer kind per axis (BC_*)
     int box[6];                 // M(t) trimming box [x0,x1) [y0,y1) [z0,z1)
     double dxd, dyd, dzd, gamma;  // FP64 copies for pulse angles and k phases
     const StepInfo* steps;      // [(nsched + 1) * nbatch], step-major
@@ -99,6 +113,9 @@ struct StepParams {
     const T* fw;
     long long fstride;
     const T* orig[3];           // MacCormack corrector: the step's input field M
+    // FP32 fast path: polls before a plane-ring wait gives up (RING_WAIT_POLLS
+    // unless a test shortens it to see the timeout path run)
+    uint32_t wait_polls;
 };
 
 // TMA descriptors of the FP32 fast path (one per ping-pong input side)

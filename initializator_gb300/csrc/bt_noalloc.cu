@@ -29,6 +29,8 @@
 #include <cstring>
 #include <mutex>
 
+#include <cudaTypedefs.h>
+
 #include "../../include/bt.h"
 #include "bt_internal.h"
 
@@ -49,22 +51,53 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_mutex;
-unsigned char* g_scratch_addr[MAX_DEVICES] = {};  // device address of the array, per device
+// per device: the device address of the array and the id of the context it
+// was looked up in (a cudaDeviceReset ends that context; the module is loaded
+// again in the next one and the array may move)
+unsigned char* g_scratch_addr[MAX_DEVICES] = {};
+unsigned long long g_scratch_ctx[MAX_DEVICES] = {};
 
-// Set-up, once per device, with that device current: the host-side name of a
-// __device__ array is only a stand-in; the address a kernel may use comes from
-// cudaGetSymbolAddress.
+// unique id of the calling thread's current context (0 when there is none or
+// the driver cannot say)
+unsigned long long current_context_id() {
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+        looked = true;
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// Set-up, once per device and context, with that device current: the
+// host-side name of a __device__ array is only a stand-in; the address a
+// kernel may use comes from cudaGetSymbolAddress (which also creates the
+// device's context on a first call).
 cudaError_t scratch_for_current_device(unsigned char** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
         g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+        g_scratch_ctx[dev] = current_context_id();
     }
     *out = g_scratch_addr[dev];
     return cudaSuccess;
@@ -177,6 +210,12 @@ extern "C" int bt_step_noalloc(const bt_config* cfg, const uint8_t* mask, const 
         return BT_E_ARG;
     for (int a = 0; a < 3; ++a)
         if (c.buffer[a] < 0 || 2 * c.buffer[a] > (a == 0 ? c.nx : a == 1 ? c.ny : c.nz)) return BT_E_ARG;
+    // one field per call, advection on or off: a batched config (a q-sweep)
+    // is not accepted, so no caller mistakes one stepped member for the batch
+    if (c.batch > 1 || c.batch < 0 || (c.velocity != 0 && c.velocity != 1)) return BT_E_ARG;
+    // a single step has no earlier step to have set non-copy ghost layers
+    // (the first step of a run reads copies): copy faces only
+    if (c.boundary[0] != BT_BC_COPY || c.boundary[1] != BT_BC_COPY || c.boundary[2] != BT_BC_COPY) return BT_E_ARG;
     if (c.velocity == 1 && (!vx || !vy || !vz)) return BT_E_ARG;
     const long long nvox = (long long)c.nx * c.ny * c.nz;
     if (nvox > BT_NOALLOC_MAX_VOXELS) {

@@ -120,6 +120,35 @@ __device__ __forceinline__ void lab_phase(double k, int c, double d, T& re, T& i
     }
 }
 
+// Ghost values of the domain faces that are not copy faces (bt_config.boundary):
+// zero, or the far edge cell (periodic), in the k frame times the face's wrap
+// factor (KSPACE). nb[c][q]: the voxel's neighbours -x +x -y +y -z +z per
+// component, holding the copy ghost on domain faces; open[q] becomes true for
+// every face given a value here. far[q]: offset of face q's far edge cell.
+template <typename T, int SCHEME>
+__device__ __forceinline__ void face_ghosts(const int (&bc)[3], const StepInfo* si, const T* const (&in)[3],
+                                            const long long (&far)[6], T (&nb)[3][6], bool (&open)[6]) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const int kind = bc[q >> 1];
+        if (open[q] || kind == BC_COPY) continue;
+        T v[3] = {(T)0, (T)0, (T)0};
+        if (kind == BC_PERIODIC) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[c] = in[c][far[q]];
+            if constexpr (SCHEME == SCHEME_KSPACE) {
+                const T wr = (T)si->wrap[q >> 1][0], wi = (q & 1) ? (T)-si->wrap[q >> 1][1] : (T)si->wrap[q >> 1][1];
+                const T re = v[0], im = v[1];
+                v[0] = wr * re - wi * im;
+                v[1] = wr * im + wi * re;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nb[c][q] = v[c];
+        open[q] = true;
+    }
+}
+
 // End of a step, shared by the step kernels: the CTA's sums (FP64) go to its
 // slot of the partials (grouped per batch member); the last CTA of the launch
 // reduces each member's partials in a fixed order (one warp per member, so
@@ -371,6 +400,10 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
     }
     const int npulse = si->pulse_count;
     const DevPulse* pulses = P.pulses + si->pulse_first;
+    // non-copy domain faces take their own ghosts from the second step on (the
+    // first step of a run from step 0 reads the reference's initial copies)
+    const int bcs[3] = {P.bc[0], P.bc[1], P.bc[2]};
+    const bool bc_live = (bcs[0] | bcs[1] | bcs[2]) != 0 && step > 0;
 
     const bool in_box = x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3];
     Acc<T> accx, accy, accz;
@@ -454,11 +487,17 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
                     nb[c][4] = cb[c];
                     nb[c][5] = ca[c];
                 }
+                bool open[6] = {x > 0, x < nx - 1, y > 0, y < ny - 1, z > 0, z < nz - 1};
+                if (bc_live) {
+                    const long long far[6] = {oz + (long long)yc * pitch + (nx - 1), oz + (long long)yc * pitch,
+                                              oz + (long long)(ny - 1) * pitch + xc, oz + xc,
+                                              (long long)(nz - 1) * plane + col, col};
+                    face_ghosts<T, SCHEME>(bcs, si, in, far, nb, open);
+                }
                 if constexpr (SCHEME == SCHEME_KSPACE) {
                     // transverse neighbours in the frame of this voxel:
-                    // phi_f * m_nb inside the domain; the voxel itself outside
-                    // (copy ghost -> zero difference)
-                    const bool open[6] = {x > 0, x < nx - 1, y > 0, y < ny - 1, z > 0, z < nz - 1};
+                    // phi_f * m_nb inside the domain and for the ghosts set
+                    // above; the voxel itself on a copy face (zero difference)
 #pragma unroll
                     for (int q = 0; q < 6; ++q) {
                         const T re = nb[0][q], im = nb[1][q];

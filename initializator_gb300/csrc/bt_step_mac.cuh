@@ -15,7 +15,8 @@
 // difference a solid neighbour holds the voxel's own value: the reference
 // writes it there first (a reflection; with several writers its GPU result is
 // racy, this is the zero-flux reading). Copy ghosts at the domain faces come
-// from index clamping, as in step_kernel. Same tile and z-march as step_kernel.
+// from index clamping, as in step_kernel; periodic and zero faces
+// (bt_config.boundary) from face_ghosts. Same tile and z-march as step_kernel.
 #pragma once
 #include "bt_step.cuh"
 
@@ -64,6 +65,12 @@ __global__ void __launch_bounds__(NTHREADS) mac_kernel(const __grid_constant__ S
     }
     const int npulse = STAGE == 1 ? si->pulse_count : 0;
     const DevPulse* pulses = P.pulses + si->pulse_first;
+    // non-copy domain faces: the predictor reads the field's ghosts, which
+    // hold the reference's initial copies in the first step of a run from
+    // step 0 (ghost layers are set at the end of each step); the corrector
+    // reads the predictor's, set right after the predictor in every step
+    const int bcs[3] = {P.bc[0], P.bc[1], P.bc[2]};
+    const bool bc_live = (bcs[0] | bcs[1] | bcs[2]) != 0 && (STAGE == 1 || step > 0);
     const bool in_box = x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3];
     Acc<T> accx, accy, accz;
 
@@ -137,6 +144,13 @@ __global__ void __launch_bounds__(NTHREADS) mac_kernel(const __grid_constant__ S
                     nbv[c][3] = sm[c][ty + 2][tx + 1];
                     nbv[c][4] = cb[c];
                     nbv[c][5] = ca[c];
+                }
+                if (bc_live) {
+                    bool open[6] = {x > 0, x < nx - 1, y > 0, y < ny - 1, z > 0, z < nz - 1};
+                    const long long far[6] = {oz + (long long)yc * pitch + (nx - 1), oz + (long long)yc * pitch,
+                                              oz + (long long)(ny - 1) * pitch + xc, oz + xc,
+                                              (long long)(nz - 1) * plane + col, col};
+                    face_ghosts<T, SCHEME_REF>(bcs, si, in, far, nbv, open);
                 }
                 T dxm = (f & 1) ? P.dps : P.dpp, dxp = (f & 2) ? P.dps : P.dpp;
                 T dym = (f & 4) ? P.dps : P.dpp, dyp = (f & 8) ? P.dps : P.dpp;

@@ -42,7 +42,13 @@
 //     previous step's CTA 0 wrote and which is read only after that grid has
 //     completed; no CTA waits on a fence or an atomic ticket.
 // Out-of-range TMA boxes (halo beyond the domain, plane -1 or nz) are
-// zero-filled and never used as data.
+// zero-filled; a copy face replaces them by its ghost as described above, a
+// zero face (bt_config.boundary) uses them as they are. Periodic faces (the
+// BCK instances, KSPACE only) load the far edge: the wrapped plane by TMA in
+// z, the far row / column by plain loads in the threads holding an edge in
+// y / x, moved into the voxel's k frame by the step's wrap factor. The first
+// step of a run from step 0 reads copy ghosts on every face, as the
+// reference's initial ghost layer.
 // Every mbarrier wait is bounded; a wait that gives up raises the CTA's
 // failure flag, which ends the other warps' waits too; after the march the
 // CTA then records status bit 8, drains its copies (bounded) and returns
@@ -97,7 +103,9 @@ struct Tile {
 };
 // the 128-wide tile keeps the layout the fast path was tuned with
 static_assert(Tile<128>::OFF_U == 16384 && Tile<128>::STAGE == 29696 && Tile<128>::AUX_BARS == 6208, "layout");
-constexpr uint32_t WAIT_LIMIT = 1u << 20;  // polls; a healthy copy lands in microseconds
+// the drain after a give-up always waits this long (polls) for the copies in
+// flight, so that no bulk copy lands in a CTA that has already exited
+constexpr uint32_t WAIT_LIMIT = RING_WAIT_POLLS;
 
 __device__ __forceinline__ uint32_t sa(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -172,7 +180,7 @@ static __global__ void cell_velocity_kernel(const StepParams<float> P, float* __
     }
 }
 
-template <int SCHEME, bool VEL, bool PREC, int TWV>
+template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK>
 __global__ void __launch_bounds__(tma::NT, 2)
     step_tma_kernel(const __grid_constant__ StepParams<float> P, const __grid_constant__ TmaMaps M, int first) {
     using namespace tma;
@@ -229,8 +237,18 @@ __global__ void __launch_bounds__(tma::NT, 2)
         if constexpr (VEL) tma_load_4d(base + OFF_U, &M.ucell, bar, x0, y0, plane, 0);
         tma_load_3d(base + OFF_CODE, &M.code, bar, x0, y0, plane);
     };
-    // plane sequence: q = 0 is the ghost-side plane, then the chunk in marching order
-    auto plane_of = [&](int q) { return d > 0 ? z0 - 1 + q : z1 - q; };
+    // ghost-layer kinds of this step (BCK instances; the first step of a run
+    // from step 0 reads copies), set once the step index is known
+    int kx = BC_COPY, ky = BC_COPY, kz = BC_COPY;
+    // plane sequence: q = 0 is the ghost-side plane, then the chunk in marching
+    // order; a periodic z face takes the far edge plane instead of plane -1 / nz
+    auto plane_of = [&](int q) {
+        int pl = d > 0 ? z0 - 1 + q : z1 - q;
+        if constexpr (BCK) {
+            if (kz == BC_PERIODIC) pl = pl < 0 ? nz - 1 : (pl >= nz ? 0 : pl);
+        }
+        return pl;
+    };
     // the host never makes an empty chunk; a CTA that still gets one issues
     // no copy, waits on nothing and contributes zero sums
     const bool empty = z1 <= z0;
@@ -273,6 +291,13 @@ __global__ void __launch_bounds__(tma::NT, 2)
     const long long step = first ? __ldcg(&P.ctl->step) : __ldcg(&P.ctl->fstep[P.side]);
     if (cta0 && tid == 0) P.ctl->fstep[1 - P.side] = step + 1;
     const StepInfo* si = P.steps + (step < P.nsched ? step : P.nsched) * nb + b;
+    if constexpr (BCK) {
+        if (step > 0) {
+            kx = P.bc[0];
+            ky = P.bc[1];
+            kz = P.bc[2];
+        }
+    }
     if (tid == 0)
         for (int q = 0; q < NSTAGE && q < nplanes; ++q) {
             issue(q, plane_of(q));
@@ -348,8 +373,9 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // warp-uniform bounded wait for the copy into `slot` at phase parity
     // `par`; false when it gave up or another thread of the CTA raised the
     // failure flag
+    const uint32_t polls = P.wait_polls;
     auto wait_full = [&](int slot, uint32_t par) -> bool {
-        for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+        for (uint32_t i = 0; i < polls; ++i) {
             if (__all_sync(0xffffffffu, mbar_try_wait(&bars[slot], par))) return true;
             if (__any_sync(0xffffffffu, vflag[0] != 0)) return false;
         }
@@ -365,7 +391,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // has released plane p - NSTAGE from it, whose phase parity is `par`
     // (bounded; raises the flag on timeout)
     auto refill = [&](int p, int slot, uint32_t par) {
-        for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+        for (uint32_t i = 0; i < polls; ++i) {
             if (mbar_try_wait(&empties[slot], par)) {
                 fence_proxy_async();
                 issue(slot, plane_of(p));
@@ -411,6 +437,22 @@ __global__ void __launch_bounds__(tma::NT, 2)
 #pragma unroll
         for (int i = 0; i < QX; ++i) ghost(g[0][i], g[1][i], g[2][i], cur[0][i], cur[1][i], cur[2][i], a, upper);
     };
+    // a periodic face's ghost: the far edge cell (mr, mi, mz) moved across the
+    // period into the k frame (exp(-i k_a L_a) below, its conjugate above)
+    auto wrap = [&](float& gr, float& gi, float& gz, float mr, float mi, float mz, int a, bool upper) {
+        if constexpr (SCHEME == SCHEME_KSPACE) {
+            const float c = si->wrapf[a][0], s_ = upper ? -si->wrapf[a][1] : si->wrapf[a][1];
+            gr = c * mr - s_ * mi;
+            gi = c * mi + s_ * mr;
+        } else {
+            gr = mr;
+            gi = mi;
+        }
+        gz = mz;
+    };
+    // input field of this member (periodic faces read the far edge directly)
+    const float* fin[3] = {P.in[0] + (long long)b * P.bstride, P.in[1] + (long long)b * P.bstride,
+                           P.in[2] + (long long)b * P.bstride};
 
     // output offset of this thread's row in plane 0
     const long long obase = (long long)b * P.bstride + (long long)y * P.pitch + xb;
@@ -455,19 +497,69 @@ __global__ void __launch_bounds__(tma::NT, 2)
         // voxels on a domain face in x or y: the halo value beyond the face
         // (zero-filled by the copy) becomes the face's ghost, so no weight
         // needs zeroing per voxel
-        if (x_lo) ghost(xm[0][0], xm[1][0], xm[2][0], cur[0][0], cur[1][0], cur[2][0], 0, false);
+        // (a zero face keeps the zero-filled halo)
+        const long long zoff = (long long)z * P.plane;
+        if (x_lo) {
+            if (kx == BC_COPY) ghost(xm[0][0], xm[1][0], xm[2][0], cur[0][0], cur[1][0], cur[2][0], 0, false);
+            if constexpr (BCK) {
+                if (kx == BC_PERIODIC) {
+                    const long long o = zoff + (long long)y * P.pitch + (nx - 1);
+                    wrap(xm[0][0], xm[1][0], xm[2][0], fin[0][o], fin[1][o], fin[2][o], 0, false);
+                }
+            }
+        }
         if (x_hi) {
 #pragma unroll
             for (int i = 0; i < QX; ++i)
-                if (xb + i == nx - 1) ghost(xp[0][i], xp[1][i], xp[2][i], cur[0][i], cur[1][i], cur[2][i], 0, true);
+                if (xb + i == nx - 1) {
+                    if (kx == BC_COPY) ghost(xp[0][i], xp[1][i], xp[2][i], cur[0][i], cur[1][i], cur[2][i], 0, true);
+                    if constexpr (BCK) {
+                        if (kx == BC_PERIODIC) {
+                            const long long o = zoff + (long long)y * P.pitch;
+                            wrap(xp[0][i], xp[1][i], xp[2][i], fin[0][o], fin[1][o], fin[2][o], 0, true);
+                        }
+                    }
+                }
         }
         if (y == 0) {
+            if (ky == BC_COPY) {
 #pragma unroll
-            for (int i = 0; i < QX; ++i) ghost(ym[0][i], ym[1][i], ym[2][i], cur[0][i], cur[1][i], cur[2][i], 1, false);
+                for (int i = 0; i < QX; ++i)
+                    ghost(ym[0][i], ym[1][i], ym[2][i], cur[0][i], cur[1][i], cur[2][i], 1, false);
+            }
+            if constexpr (BCK) {
+                if (ky == BC_PERIODIC) {
+                    const long long o = zoff + (long long)(ny - 1) * P.pitch + xb;
+                    float f[3][QX];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float4 v = *reinterpret_cast<const float4*>(fin[c] + o);
+                        f[c][0] = v.x; f[c][1] = v.y; f[c][2] = v.z; f[c][3] = v.w;
+                    }
+#pragma unroll
+                    for (int i = 0; i < QX; ++i) wrap(ym[0][i], ym[1][i], ym[2][i], f[0][i], f[1][i], f[2][i], 1, false);
+                }
+            }
         }
         if (y == ny - 1) {
+            if (ky == BC_COPY) {
 #pragma unroll
-            for (int i = 0; i < QX; ++i) ghost(yp[0][i], yp[1][i], yp[2][i], cur[0][i], cur[1][i], cur[2][i], 1, true);
+                for (int i = 0; i < QX; ++i)
+                    ghost(yp[0][i], yp[1][i], yp[2][i], cur[0][i], cur[1][i], cur[2][i], 1, true);
+            }
+            if constexpr (BCK) {
+                if (ky == BC_PERIODIC) {
+                    const long long o = zoff + xb;
+                    float f[3][QX];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float4 v = *reinterpret_cast<const float4*>(fin[c] + o);
+                        f[c][0] = v.x; f[c][1] = v.y; f[c][2] = v.z; f[c][3] = v.w;
+                    }
+#pragma unroll
+                    for (int i = 0; i < QX; ++i) wrap(yp[0][i], yp[1][i], yp[2][i], f[0][i], f[1][i], f[2][i], 1, true);
+                }
+            }
         }
         const uint32_t code4 = *reinterpret_cast<const uint32_t*>(base + OFF_CODE + row * TW + QX * xl);
         float ux[QX] = {0.f, 0.f, 0.f, 0.f}, uy[QX] = {0.f, 0.f, 0.f, 0.f}, uz[QX] = {0.f, 0.f, 0.f, 0.f};
@@ -577,9 +669,28 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
         };
         // planes on a domain face in z: the ghost plane beyond it (zero-filled
-        // by the copy, used by nothing else) becomes the face's ghost
-        if (z == 0) ghost_plane(d > 0 ? prv : nxt, 2, false);
-        if (z == nz - 1) ghost_plane(d > 0 ? nxt : prv, 2, true);
+        // by the copy, used by nothing else) becomes the face's ghost; on a
+        // periodic face it is the far edge plane, moved into the k frame
+        if (z == 0) {
+            if (kz == BC_COPY) ghost_plane(d > 0 ? prv : nxt, 2, false);
+            if constexpr (BCK) {
+                if (kz == BC_PERIODIC) {
+                    float (&g)[3][QX] = d > 0 ? prv : nxt;
+#pragma unroll
+                    for (int i = 0; i < QX; ++i) wrap(g[0][i], g[1][i], g[2][i], g[0][i], g[1][i], g[2][i], 2, false);
+                }
+            }
+        }
+        if (z == nz - 1) {
+            if (kz == BC_COPY) ghost_plane(d > 0 ? nxt : prv, 2, true);
+            if constexpr (BCK) {
+                if (kz == BC_PERIODIC) {
+                    float (&g)[3][QX] = d > 0 ? nxt : prv;
+#pragma unroll
+                    for (int i = 0; i < QX; ++i) wrap(g[0][i], g[1][i], g[2][i], g[0][i], g[1][i], g[2][i], 2, true);
+                }
+            }
+        }
         if (d > 0) body(prv, nxt);
         else body(nxt, prv);
         release(sc);
@@ -641,19 +752,19 @@ static inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, int smem, cud
     return cfg;
 }
 
-template <int SCHEME, bool VEL, bool PREC, int TWV>
+template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK = false>
 static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, bool first, cudaStream_t s) {
     constexpr int smem = tma::Tile<TWV>::SMEM;
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV>,
+        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         configured = true;
     }
     cudaLaunchAttribute attr[1];
     const cudaLaunchConfig_t cfg = pdl_config(grid, dim3(tma::NT), smem, s, attr);
-    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV>, p, m, first ? 1 : 0);
+    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK>, p, m, first ? 1 : 0);
 }
 
 // the fast path's kernels of one tile width
@@ -665,6 +776,11 @@ static cudaError_t launch_step_tma_w(const StepParams<float>& p, const TmaMaps& 
         if (vel) return launch_tma_t<SCHEME_REF, true, false, TWV>(p, m, grid, first, s);
         if (prec) return launch_tma_t<SCHEME_REF, false, true, TWV>(p, m, grid, first, s);
         return launch_tma_t<SCHEME_REF, false, false, TWV>(p, m, grid, first, s);
+    }
+    // KSPACE with a non-copy face: the instance that reads the far edge
+    if (p.bc[0] != BC_COPY || p.bc[1] != BC_COPY || p.bc[2] != BC_COPY) {
+        if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, true>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_KSPACE, false, false, TWV, true>(p, m, grid, first, s);
     }
     if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV>(p, m, grid, first, s);
     return launch_tma_t<SCHEME_KSPACE, false, false, TWV>(p, m, grid, first, s);

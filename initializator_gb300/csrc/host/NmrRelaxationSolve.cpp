@@ -257,6 +257,20 @@ bt_config NmrRelaxationSolve::make_config(bool gpu_path) const {
     c.rho1 = water ? d.r1Water : d.r1Oil;
     c.rho2 = water ? d.r2Water : d.r2Oil;
     c.p_eq = pEq_;
+    // ghost layers: the CPU path (solve, ExplicitSimple) copies on every face
+    // whatever Nmr_data.dat says (BoundaryConditionsForVectorField,
+    // cpp:1664-1754); the GPU path dispatches on nBoundary1..6 (cu:1321-1396):
+    // per pair (x: 1 and 3, y: 2 and 4, z: 5 and 6) copy when both are 1,
+    // periodic when both are 3, and zero otherwise (BC_Advanced on x for a 2;
+    // a pair that routine leaves alone keeps never-written, zero ghosts)
+    for (int a = 0; a < 3; ++a) c.boundary[a] = BT_BC_COPY;
+    if (gpu_path) {
+        const int lo[3] = {d.nb[0], d.nb[1], d.nb[4]}, hi[3] = {d.nb[2], d.nb[3], d.nb[5]};
+        for (int a = 0; a < 3; ++a)
+            c.boundary[a] = (lo[a] == 1 && hi[a] == 1) ? BT_BC_COPY
+                            : (lo[a] == 3 && hi[a] == 3) ? BT_BC_PERIODIC
+                                                         : BT_BC_ZERO;
+    }
     return c;
 }
 
@@ -287,11 +301,6 @@ void NmrRelaxationSolve::initial_field(std::vector<double>& mx, std::vector<doub
 void NmrRelaxationSolve::run(bool gpu_path) {
     if (!initialised_) die("init() must come before solve()");
     const nmr::Data& d = data_;
-    if (gpu_path)
-        for (int b = 0; b < 6; ++b)
-            if (d.nb[b] != 1)
-                std::cout << "NB" << (b + 1) << " = " << d.nb[b]
-                          << ": only zero-derivative (copy) boundaries are implemented; using them" << std::endl;
     const bt_config c = make_config(gpu_path);
     check(bt_create(&c, &h_), "bt_create");
     check(bt_upload_geometry(h_, mask_.data(), vx_.empty() ? nullptr : vx_.data(), vy_.empty() ? nullptr : vy_.data(),

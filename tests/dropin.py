@@ -13,12 +13,14 @@ DRIVER_SRC = os.path.join(ROOT, "tests", "drivers", "describe_init.cpp")
 DRIVER = os.path.join(ROOT, "initializator_gb300", "_build", "describe_init")
 
 
-def write_case_dir(case, path):
-    """The fixture's reference input directory (data/*.dat) under path."""
+def write_case_dir(case, path, **overrides):
+    """The fixture's reference input directory (data/*.dat) under path;
+    overrides replace Nmr_data.dat parameters (NmrData field names)."""
     from initializator_gb300 import datfiles
     z = load(case)
     kw = {f.name: type(getattr(datfiles.NmrData(), f.name))(z["data_" + f.name].item())
           for f in dataclasses.fields(datfiles.NmrData)}
+    kw.update(overrides)
     data = datfiles.NmrData(**kw)
     vel = (z["vx"], z["vy"], z["vz"]) if data.n_velocity == 1 else None
     surf = {}

@@ -119,3 +119,41 @@ def test_nmr_exe_end_to_end(case, path, tmp_path, btlib, oracle_lib):
 def _read_csv_noheader(path):
     with open(path) as f:
         return np.array([float(v) for v in f.readline().split(";")])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nb", [(3, 3, 3, 3, 3, 3), (2, 1, 1, 1, 3, 3), (1, 3, 3, 1, 1, 1)])
+@pytest.mark.parametrize("case", ["fid", "pfg_flow"])
+def test_nmr_exe_boundaries(case, nb, tmp_path, btlib, oracle_lib):
+    """solve_gpu with nBoundary1..6 other than 1: the drop-in maps them to the
+    GPU path's ghost-layer kinds (copy / periodic / zero per pair); its CSV
+    matches the oracle's MacCormack run with those kinds (which the GPU tests
+    pin to the reference's own BC kernels) to 5e-6 relative. solve() (the CPU
+    path) keeps copy layers, as the reference's CPU path does."""
+    import initializator_gb300 as bt
+    import oracle
+    from initializator_gb300 import build
+    ov = {f"nb{b + 1}": int(v) for b, v in enumerate(nb)}
+    z = write_case_dir(case, str(tmp_path), **ov)
+    d = describe(str(tmp_path))
+    r = subprocess.run([build.EXE, "1", "1", "1"], cwd=str(tmp_path), capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    got = _read_csv(os.path.join(str(tmp_path), "results_gpu.csv"))
+    dt = d["dTime"][0]
+    nstep = int(d["nStep"][0])
+    kw = common(z)
+    kw["dt"] = dt
+    pl = bt.sequence_schedule(int(z["data_n_sequence"]), nstep + 1, dt=dt, time1=float(z["data_time1"]),
+                              time2=float(z["data_time2"]), direction=tuple(z["direction"]),
+                              gradient_pulse=float(z["gradient_pulse"]), gpu_variant=True)
+    p = oracle.make_params(z["mask"].shape, boundary=bt.boundary_from_nb(nb), **kw)
+    _, mt = oracle.run(p, z["mask"], initial_state(z), nstep + 1, vel=velocity(z), pulses=pl, maccormack=True)
+    nd = int(z["data_nd_print"])
+    steps = np.arange(0, nstep + 1, nd)
+    ref = mt[steps]
+    assert got.shape == (len(steps), 4)
+    assert np.abs(got[:, 1:] - ref).max() <= 5e-6 * np.abs(ref).max()
+    # the same case with copy layers gives another curve: the kinds took effect
+    p0 = oracle.make_params(z["mask"].shape, **kw)
+    _, mt0 = oracle.run(p0, z["mask"], initial_state(z), nstep + 1, vel=velocity(z), pulses=pl, maccormack=True)
+    assert np.abs(mt0[steps] - ref).max() > 1e-4 * np.abs(ref).max()
