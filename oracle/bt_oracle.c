@@ -80,6 +80,37 @@ static void bc_copy_d(const grid_t* g, double* f) {
         }
 }
 
+/* ghost layers per axis (x, then y, then z, each over the full extent of the
+ * other two axes): 0 copy of the neighbouring cell (BC_ZeroDer_*,
+ * src/NmrRelaxationSolveKernels.cu:969-1000), 1 periodic, the far interior
+ * plane (BC_Inf_*, cu:1002-1033), 2 zero (BC_Advanced_XM/XP with Val 0,
+ * cu:1035-1053; the GPU path also leaves zero in the ghosts of a pair it does
+ * not handle, cu:1321-1396) */
+static void bc_apply_d(const grid_t* g, double* f, const int mode[3]) {
+    int nx = g->nx, ny = g->ny, nz = g->nz;
+    for (int k = 0; k < nz + 2; k++)
+        for (int j = 0; j < ny + 2; j++) {
+            size_t lo = gidx(g, 0, j, k), hi = gidx(g, nx + 1, j, k);
+            if (mode[0] == 1) { f[lo] = f[gidx(g, nx, j, k)]; f[hi] = f[gidx(g, 1, j, k)]; }
+            else if (mode[0] == 2) { f[lo] = 0.0; f[hi] = 0.0; }
+            else { f[lo] = f[gidx(g, 1, j, k)]; f[hi] = f[gidx(g, nx, j, k)]; }
+        }
+    for (int k = 0; k < nz + 2; k++)
+        for (int i = 0; i < nx + 2; i++) {
+            size_t lo = gidx(g, i, 0, k), hi = gidx(g, i, ny + 1, k);
+            if (mode[1] == 1) { f[lo] = f[gidx(g, i, ny, k)]; f[hi] = f[gidx(g, i, 1, k)]; }
+            else if (mode[1] == 2) { f[lo] = 0.0; f[hi] = 0.0; }
+            else { f[lo] = f[gidx(g, i, 1, k)]; f[hi] = f[gidx(g, i, ny, k)]; }
+        }
+    for (int j = 0; j < ny + 2; j++)
+        for (int i = 0; i < nx + 2; i++) {
+            size_t lo = gidx(g, i, j, 0), hi = gidx(g, i, j, nz + 1);
+            if (mode[2] == 1) { f[lo] = f[gidx(g, i, j, nz)]; f[hi] = f[gidx(g, i, j, 1)]; }
+            else if (mode[2] == 2) { f[lo] = 0.0; f[hi] = 0.0; }
+            else { f[lo] = f[gidx(g, i, j, 1)]; f[hi] = f[gidx(g, i, j, nz)]; }
+        }
+}
+
 static void bc_copy_c(const grid_t* g, char* f) {
     int nx = g->nx, ny = g->ny, nz = g->nz;
     for (int k = 0; k < nz + 2; k++)
@@ -535,7 +566,7 @@ static int run_impl(const bto_params* p, const uint8_t* mask,
             for (size_t q = 0; q < g->num; q++) { f.ax[q] = 0.0; f.ay[q] = 0.0; f.az[q] = 0.0; }
             #pragma omp parallel for schedule(static)
             for (int k = 1; k <= g->nz; k++) mac_plane(p, &f, k, G, 0, f.mx, f.my, f.mz, f.ax, f.ay, f.az);
-            bc_copy_d(g, f.ax); bc_copy_d(g, f.ay); bc_copy_d(g, f.az);
+            bc_apply_d(g, f.ax, p->boundary); bc_apply_d(g, f.ay, p->boundary); bc_apply_d(g, f.az, p->boundary);
             #pragma omp parallel for schedule(static)
             for (int k = 1; k <= g->nz; k++) mac_plane(p, &f, k, G, 1, f.ax, f.ay, f.az, cx, cy, cz);
             #pragma omp parallel for schedule(static)
@@ -557,7 +588,7 @@ static int run_impl(const bto_params* p, const uint8_t* mask,
         if (p->vector_mult == 2) precess_exact(p, &f, G);
         for (int q = 0; q < npulses; q++)
             if (pulses[q].step == s) add_impulse(p, &f, &pulses[q]);
-        bc_copy_d(g, f.mx); bc_copy_d(g, f.my); bc_copy_d(g, f.mz);
+        bc_apply_d(g, f.mx, p->boundary); bc_apply_d(g, f.my, p->boundary); bc_apply_d(g, f.mz, p->boundary);
         if (mt) field_sums(p, g, f.act, f.mx, f.my, f.mz, &mt[3 * s], scratch);
         if (mt6) phase_sums(p, g, f.act, c1, c2, f.mx, f.my, f.mz, &mt6[6 * s]);
     }
@@ -633,4 +664,35 @@ void bto_rates(const bto_params* p, const uint8_t* mask, double* tau1, double* t
             }
     ofields_free(&f);
     free(z);
+}
+
+int bto_gpu_inputs(const bto_params* p, const uint8_t* mask,
+                   const double* vx, const double* vy, const double* vz,
+                   const double* mx, const double* my, const double* mz,
+                   char* act, double* diff, double* t1, double* t2,
+                   double* nf, double* vel, double* magn) {
+    if (!p || p->nx <= 0 || p->ny <= 0 || p->nz <= 0) return -1;
+    ofields_t f;
+    if (ofields_init(p, mask, vx, vy, vz, mx, my, mz, &f)) return -2;
+    const grid_t* g = &f.g;
+    const size_t num = g->num;
+    for (size_t q = 0; q < num; q++) {
+        act[q] = f.act[q] ? '1' : '0';
+        diff[q] = f.D[q];
+        t1[q] = f.t1[q] != 0.0 ? f.t1[q] : BIG;
+        t2[q] = f.t2[q] != 0.0 ? f.t2[q] : BIG;
+        vel[q] = f.vx[q]; vel[num + q] = f.vy[q]; vel[2 * num + q] = f.vz[q];
+        magn[q] = f.mx[q]; magn[num + q] = f.my[q]; magn[2 * num + q] = f.mz[q];
+    }
+    /* FillInMainField (cpp:1944-1972): G * d * (i - 0.5) over every ghosted index */
+    for (int k = 0; k < g->nz + 2; k++)
+        for (int j = 0; j < g->ny + 2; j++)
+            for (int i = 0; i < g->nx + 2; i++) {
+                size_t c = gidx(g, i, j, k);
+                nf[c] = p->grad[0] * p->dx * (i - 0.5);
+                nf[num + c] = p->grad[1] * p->dy * (j - 0.5);
+                nf[2 * num + c] = p->grad[2] * p->dz * (k - 0.5);
+            }
+    ofields_free(&f);
+    return 0;
 }

@@ -36,6 +36,12 @@ typedef struct {
     int velocity;            /* nVelocity */
     int diffusion;           /* nDiffusion */
     int buffer[3];           /* bufferX/Y/Z trimming of the M(t) sums */
+    int boundary[3];         /* ghost layers per axis x, y, z after each step (and after the
+                                MacCormack predictor): 0 copy (BC_ZeroDer_*, the CPU path's only
+                                kind), 1 periodic (BC_Inf_*), 2 zero (BC_Advanced_XM/XP with 0,
+                                and the never-written ghosts of pairs the GPU path leaves alone);
+                                the first step reads the initial copy ghosts, as the reference's
+                                arrays hold them before its first step */
 } bto_params;
 
 /* An instantaneous pulse applied after the update of step `step`
@@ -81,6 +87,20 @@ int bto_run_maccormack(const bto_params* p, const uint8_t* mask,
                        long long nsteps, const bto_pulse* pulses, int npulses, const double* grad_wave,
                        const double* t1, const double* t2, const double* diff,
                        const double* c1, const double* c2, double* mt, double* mt6, int threads);
+
+/* The ghosted arrays the reference's GPU path starts from (what InitializeGpu,
+ * src/NmrRelaxationSolveKernels.cu:12-88, copies to the device), for running
+ * its own kernels: num = (nx+2)(ny+2)(nz+2) cells, x fastest. act: '0'/'1'
+ * with the copy ghost layer (BoundaryConditionsForActiveCells); diff, t1, t2:
+ * FillInDiffusinAndTime (ghost layer of diff copied; t1, t2 ghosts 1e50, never
+ * read); nf: FillInMainField's gradient field G*d*(i - 0.5) (3*num, x y z);
+ * vel: ReadVelocity's face velocities (3*num); magn: the field with copy
+ * ghosts (3*num). Returns 0 on success. */
+int bto_gpu_inputs(const bto_params* p, const uint8_t* mask,
+                   const double* vx, const double* vy, const double* vz,
+                   const double* mx, const double* my, const double* mz,
+                   char* act, double* diff, double* t1, double* t2,
+                   double* nf, double* vel, double* magn);
 
 /* Wall time (s) of the stepping loop of the last bto_run_reference call. */
 double bto_last_loop_seconds(void);
