@@ -256,13 +256,58 @@ def run_c1(args, lr):
 
 C5_SHAPE = (768, 1024, 1024)  # C5: 1024 x 1024 x 768
 C5_STEPS = 500
+C5_ERR_STEPS = 200            # FP32-vs-FP64 horizon at C5 (the FP64 path runs ~4 G voxel-steps/s)
+C2_ERR_STEPS = 5000           # the whole 5000-step C2 run
+MT_ERR_TOL = 1e-4             # the plain form's FP32 M(t) bar
+
+
+def mt_error_vs_f64(shape, mask, vel, kw, wave, rf, nsteps, device=None):
+    """The benched FP32 kernel's M(t) against an FP64 run of the same solver
+    (KSPACE scheme, same geometry, flow, waveform and pulses, same start:
+    Mx = 1 in the pores): max over the nsteps steps of |M_FP32(t) - M_FP64(t)|
+    (the 3-vector) divided by |M_FP64(0)|. The FP64 run is the generic kernel
+    (pinned to the oracle's exact-rotation mode), the FP32 run the TMA fast
+    path with the generic kernel on pulse steps, as in the timed region.
+    Inputs on the host (numpy) or, with device set, the mask as a torch
+    tensor on that device (the field is then set from device memory)."""
+    import torch
+
+    import initializator_gb300 as bt
+    mts, secs = {}, {}
+    for name, prec in (("f32", bt.BT_F32), ("f64", bt.BT_F64)):
+        s = bt.Solver(bt.make_config(shape, precision=prec, scheme=bt.BT_SCHEME_KSPACE, **kw))
+        try:
+            s.upload_geometry(mask, vel)
+            s.set_schedule(rf, grad_wave=wave[:nsteps + 1])
+            dt = torch.float64 if prec == bt.BT_F64 else torch.float32
+            m = torch.as_tensor(mask, device=device or "cuda").to(dt).contiguous()
+            z = torch.zeros_like(m)
+            s.set_state_device([m, z, z.clone()])
+            del m, z
+            m0 = s.measure()
+            t0 = time.perf_counter()
+            mt = s.run(nsteps)
+            secs[name] = time.perf_counter() - t0
+            mts[name] = (m0, mt)
+        finally:
+            s.close()
+        torch.cuda.empty_cache()
+    m0 = mts["f64"][0]
+    d = np.linalg.norm(mts["f32"][1] - mts["f64"][1], axis=1)
+    err = float(d.max() / np.linalg.norm(m0))
+    return {"steps": nsteps, "value": err, "tol": MT_ERR_TOL, "pass": err <= MT_ERR_TOL,
+            "definition": "max_t |M_f32(t) - M_f64(t)| / |M_f64(0)|, M = (Mx, My, Mz) lab-frame sums",
+            "f64_seconds": secs["f64"], "f32_seconds": secs["f32"],
+            "echo_f64": [float(v) for v in mts["f64"][1][-1]]}
 
 
 def run_c5(args, lr):
     """C5, the largest single-GPU workload: 1024x1024x768 thresholded GRF
     (sigma 5, porosity 0.2), curl-noise flow up to 2 mm/s, PGSE along z with
-    G = 0.2 T/m, KSPACE FP32: ~805 M voxels, ~30 GB resident. 500 time steps
-    timed after 64 warm-up steps (one launch per step)."""
+    G = 0.2 T/m and the 180-degree refocusing pulse, KSPACE FP32: ~805 M
+    voxels, ~40 GB resident. 500 time steps timed after 64 warm-up steps, with
+    their own clock record; then the FP32-vs-FP64 M(t) error over the first
+    C5_ERR_STEPS steps from the initial field."""
     import torch
 
     import initializator_gb300 as bt
@@ -275,12 +320,12 @@ def run_c5(args, lr):
     dt = geometry.stable_dt(1e-6, 2.3e-9)
     total = 64 + C5_STEPS + 32
     wave = bt.kspace_waveform_pgse(total, dt, 0.2, 2e-3, 20e-3, axis=(0.0, 0.0, 1.0))
+    rf = [(bt.pgse_refocus_step(dt, 20e-3), 2, math.pi, (1.0, 0.0, 0.0))]
     kw = dict(dx=1e-6, dt=dt, d_pore=2.3e-9, t1=2.5, t2=2.0, rho1=1e-5, rho2=1e-5, p_eq=1.0, velocity=1,
               diffusion=1, gamma=bt.GAMMA_PROTON)
     s = bt.Solver(bt.make_config(C5_SHAPE, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, **kw))
     s.upload_geometry(mask, vel)
-    del vel
-    s.set_schedule([], grad_wave=wave)
+    s.set_schedule(rf, grad_wave=wave)
     mx = torch.as_tensor(mask, device=dev).float().contiguous()
     zero = torch.zeros_like(mx)
     s.set_state_device([mx, zero, zero.clone()])
@@ -291,19 +336,27 @@ def run_c5(args, lr):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    clocks = ClockSampler(lr)
+    clocks.start()
     ev0.record(stream)
     s.run_async(C5_STEPS)
     ev1.record(stream)
     s.synchronize()
+    clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     mt = s.read_mt(C5_STEPS)
     s.close()
+    torch.cuda.empty_cache()
+    err = mt_error_vs_f64(C5_SHAPE, mask, vel, kw, wave, rf, C5_ERR_STEPS, device=dev)
+    del vel
     nvox = int(np.prod(C5_SHAPE))
     per = ms / 1e3 / C5_STEPS
     peak, peak_kind = hbm_peak()
-    return {"workload": "C5: 1024x1024x768 GRF sigma=5 porosity 0.2, curl-noise flow 2 mm/s, PGSE z G=0.2 T/m, FP32",
+    return {"workload": "C5: 1024x1024x768 GRF sigma=5 porosity 0.2, curl-noise flow 2 mm/s, PGSE z G=0.2 T/m, "
+                        "180-degree refocusing pulse, FP32",
             "voxels": nvox, "steps": C5_STEPS, "value": nvox / per, "unit": UNIT, "ms_per_time_step": per * 1e3,
-            "tma_zsplit": zsplit, "finite": bool(np.all(np.isfinite(mt))), "generate_s": gen_s,
+            "tma_zsplit": zsplit, "finite": bool(np.all(np.isfinite(mt))), "generate_s": gen_s, "clocks": clk,
+            "mt_rel_err_vs_f64": err,
             "roofline": {"bound": "hbm", "achieved": BYTES_PER_VOXEL_STEP * nvox / per / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": BYTES_PER_VOXEL_STEP * nvox / per / 1e9 / peak,
                          "peak_kind": peak_kind, "bytes_per_voxel_step": BYTES_PER_VOXEL_STEP}}
@@ -413,6 +466,91 @@ def cpu_baseline(mask, vel, seconds=6.0):
                       f"PGSE waveform), OpenMP over z-planes, {el:.1f} s"}
 
 
+B1_STEPS = {"c1": (2000, 100), "c2": (200, 10)}  # steps timed with ndPrint = nStep, and with ndPrint = 1
+
+
+def _compat_workload(name):
+    """The MacCormack FP64 comparison workloads: C1 (64^3 sphere pack r 6, solid
+    0.35, no flow, no gradient) and C2 (the bench's 256^3 pack with its flow and
+    a static z gradient of 0.1 T/m, cross-product precession), both with the
+    reference's g and Mxy = 1 in the pores."""
+    from initializator_gb300 import geometry
+    dt = geometry.stable_dt(1e-6, 2.3e-9)
+    kw = dict(dx=1e-6, dt=dt, d_pore=2.3e-9, t1=2.5, t2=2.0, rho1=1e-5, rho2=1e-5, p_eq=1.0, diffusion=1)
+    if name == "c1":
+        mask = geometry.sphere_pack(C1_SHAPE, 6.0, 0.35, seed=SEED + 31)
+        vel = None
+        kw.update(main_field=(1.0, 0.0, 0.0), grad=(0.0, 0.0, 0.0), vector_mult=0, velocity=0)
+    else:
+        mask, vel = build_workload("cpu")
+        kw.update(main_field=(0.0, 0.0, 1.0), grad=(0.0, 0.0, 0.1), vector_mult=1, velocity=1)
+    st0 = np.zeros((3,) + mask.shape)
+    st0[0] = mask
+    return mask, vel, kw, st0
+
+
+def reference_gpu_baseline():
+    """The reference's own CUDA path at one rank: its MacCormack kernels and
+    BC kernels (compiled from its sources, nvcc's default flags as its own
+    build) driven as solve_gpu drives them (oracle/ref_gpu.cpp), FP64, at C1
+    and C2; timed with ndPrint = nStep (kernels, boundary launches and
+    device copies only) and ndPrint = 1 (plus three full-field device-to-host
+    copies and the host sums every step). Host wall clock of the loop."""
+    import torch
+
+    import oracle
+    if not torch.cuda.is_available():
+        return {"unavailable": "no GPU on this host"}
+    if oracle.ref_gpu_cubin(fmad=True) is None:
+        return {"unavailable": "the reference's kernels were not compiled into oracle/_ref (its sources are read "
+                               "only where BT_REFERENCE_DIR names them)"}
+    out = {"kind": "the reference's CUDA kernels (src/NmrRelaxationSolveKernels.cu, unmodified, nvcc default "
+                   "flags), one rank, host loop of solve_gpu restated; FP64 MacCormack", "unit": UNIT}
+    for name in ("c1", "c2"):
+        mask, vel, kw, st0 = _compat_workload(name)
+        p = oracle.make_params(mask.shape, **kw)
+        nvox = int(mask.size)
+        n_fast, n_slow = B1_STEPS[name]
+        with oracle.RefGpu(p, mask, st0, vel=vel, fmad=True) as r:
+            r.run(10, 10)  # warm-up: module load, first launches
+            _, t_fast = r.run(n_fast, n_fast)
+            _, t_slow = r.run(n_slow, 1)
+        out[name] = {"grid": list(mask.shape), "ndprint_nstep": {"steps": n_fast, "seconds": t_fast,
+                                                                "value": nvox * n_fast / t_fast},
+                     "ndprint_1": {"steps": n_slow, "seconds": t_slow, "value": nvox * n_slow / t_slow}}
+    return out
+
+
+def run_compat(args, lr):
+    """Our own MacCormack FP64 path (the drop-in solve_gpu's default) on the
+    workloads the reference's CUDA path is timed on (B1): steps on the device,
+    M(t) every step, CUDA events on the handle's stream."""
+    import torch
+
+    import initializator_gb300 as bt
+    out = {"scheme": "MacCormack FP64 (the reference's GPU scheme, bit-identical to its kernels)", "unit": UNIT}
+    for name in ("c1", "c2"):
+        mask, vel, kw, st0 = _compat_workload(name)
+        n = B1_STEPS[name][0]
+        with bt.Solver(bt.make_config(mask.shape, precision=bt.BT_F64, scheme=bt.BT_SCHEME_MACCORMACK, **kw)) as s:
+            s.upload_geometry(mask, vel)
+            s.set_state(st0)
+            s.run(64)
+            stream = torch.cuda.ExternalStream(s.stream_ptr)
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            s.run_async(n)
+            ev1.record(stream)
+            s.synchronize()
+            ms = ev0.elapsed_time(ev1)
+            mt = s.read_mt(n)
+        out[name] = {"grid": list(mask.shape), "steps": n, "value": mask.size * n / (ms / 1e3),
+                     "us_per_step": 1e3 * ms / n, "finite": bool(np.all(np.isfinite(mt)))}
+    return out
+
+
 def run_reference(args):
     r, w, _ = rank_info()
     if r != 0:
@@ -446,6 +584,7 @@ def run_reference(args):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{per} time step per bench step of the 256^3 workload, FP64, all host threads"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_gpu": reference_gpu_baseline(),
     }
     print(json.dumps(out))
 
@@ -533,10 +672,17 @@ def run_ours(args):
     e2e_s = max_over_ranks(e2e_s)
     e2e = job_value(nvox * S * args.steps, w, e2e_s)
     s.close()
+    # the benched kernel's M(t) against an FP64 run of the same solver, over
+    # the whole 5000-step C2 run (a separate waveform of that length)
+    err_c2 = None
+    if not args.no_f64_check:
+        kw2, wave2, rf2 = physics(C2_ERR_STEPS + 64)
+        err_c2 = mt_error_vs_f64(SHAPE, mask, vel, kw2, wave2, rf2, C2_ERR_STEPS)
     qsweep = None if args.no_qsweep else run_qsweep(args, lr)
     ragged = None if args.no_ragged else run_ragged(args, lr)
-    c5 = run_c5(args, lr) if args.c5 else None
+    c5 = None if args.no_c5 else run_c5(args, lr)
     c1 = run_c1(args, lr) if args.c1 else None
+    compat = None if args.no_compat else run_compat(args, lr)
 
     out = None
     if r == 0:
@@ -557,10 +703,12 @@ def run_ours(args):
                     "d2h_bytes_per_step": 3 * 8 * S},
             "gpu_launches": launches,
             "clocks": clk,
+            "mt_rel_err_vs_f64": err_c2,
             "qsweep": qsweep,
             "ragged": ragged,
             "c5": c5,
             "c1": c1,
+            "compat_f64": compat,
         }
         print(json.dumps(out))
     if w > 1:
@@ -578,7 +726,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-qsweep", action="store_true", help="skip the batched 32-gradient q-sweep (C3a) leg")
     ap.add_argument("--no-ragged", action="store_true", help="skip the 48-sample ragged batch (C3b) leg")
-    ap.add_argument("--c5", action="store_true", help="add the 1024x1024x768 (C5, ~40 GB) leg")
+    ap.add_argument("--no-c5", action="store_true", help="skip the 1024x1024x768 (C5, ~100 GB with its FP64 check) leg")
+    ap.add_argument("--no-compat", action="store_true",
+                    help="skip the MacCormack FP64 (the reference's GPU scheme) leg at C1 and C2")
+    ap.add_argument("--no-f64-check", action="store_true",
+                    help="skip the FP32-vs-FP64 M(t) error over the 5000-step C2 run")
     ap.add_argument("--c1", action="store_true", help="add the 64^3 compatibility (C1, FP64 and FP32) leg")
     ap.add_argument("--zsplit", type=int, default=0, help="fixed z-chunking of the fast path (skips the autotuner)")
     ap.add_argument("--profile", action="store_true",
