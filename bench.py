@@ -95,16 +95,17 @@ def run_qsweep(args, lr):
     mask = geometry.gaussian_random_field(QSHAPE, 3.0, 0.25, seed=SEED + 7, device=dev)
     vel = geometry.curl_velocity(mask, 4.0, 1.0e-3, seed=SEED + 8, device=dev)
     S = QSTEPS_PER_ITER
+    QB = args.qbatch
     total = (args.warmup + args.steps) * S + 64
     kw, wave, rf = physics(total)
-    amps = np.linspace(0.0, 0.3, QBATCH) / 0.1   # physics() builds the 0.1 T/m waveform
+    amps = np.linspace(0.0, 0.3, QB) / 0.1   # physics() builds the 0.1 T/m waveform
     waves = np.ascontiguousarray(wave[:, None, :] * amps[None, :, None])
-    s = bt.Solver(bt.make_config(QSHAPE, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, batch=QBATCH, **kw))
+    s = bt.Solver(bt.make_config(QSHAPE, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, batch=QB, **kw))
     s.upload_geometry(mask, vel)
     s.set_schedule(rf, grad_wave=waves)
     m = torch.from_numpy(mask).to(dev, torch.float32)
-    st = [m.expand(QBATCH, *QSHAPE).contiguous(), torch.zeros((QBATCH,) + QSHAPE, device=dev),
-          torch.zeros((QBATCH,) + QSHAPE, device=dev)]
+    st = [m.expand(QB, *QSHAPE).contiguous(), torch.zeros((QB,) + QSHAPE, device=dev),
+          torch.zeros((QB,) + QSHAPE, device=dev)]
     s.set_state_device(st)
     del st, m
     zsplit = s.autotune(8)
@@ -124,16 +125,16 @@ def run_qsweep(args, lr):
     finite = bool(np.all(np.isfinite(mt)))
     s.close()
     nvox = int(np.prod(QSHAPE))
-    vsteps = nvox * QBATCH * S * args.steps
+    vsteps = nvox * QB * S * args.steps
     per_launch = ms / 1e3 / (S * args.steps)
-    bytes_launch = (24 * QBATCH + 13) * nvox
+    bytes_launch = (24 * QB + 13) * nvox
     peak, peak_kind = hbm_peak()
     return {"workload": "C3a: 384x384x256 GRF sigma=3 porosity 0.25, flow 1 mm/s, 32 PGSE G in 0..0.3 T/m, FP32",
-            "value": vsteps / (ms / 1e3), "unit": UNIT, "ms_per_time_step": per_launch * 1e3, "batch": QBATCH,
+            "value": vsteps / (ms / 1e3), "unit": UNIT, "ms_per_time_step": per_launch * 1e3, "batch": QB,
             "tma_zsplit": zsplit, "finite": finite,
             "roofline": {"bound": "hbm", "achieved": bytes_launch / per_launch / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": bytes_launch / per_launch / 1e9 / peak, "peak_kind": peak_kind,
-                         "bytes_per_voxel_step": 24 + 13 / QBATCH}}
+                         "bytes_per_voxel_step": 24 + 13 / QB}}
 
 
 RAGGED_N = 48               # C3b: 48 independent sphere packs
@@ -735,11 +736,23 @@ def main():
     ap.add_argument("--zsplit", type=int, default=0, help="fixed z-chunking of the fast path (skips the autotuner)")
     ap.add_argument("--profile", action="store_true",
                     help="device-resident phase only (for ncu captures); prints no bench line")
+    ap.add_argument("--profile-leg", default="c2", choices=["c2", "qsweep", "ragged"],
+                    help="with --profile: the leg to run (C2's timed phase, the q-sweep or the ragged batch)")
+    ap.add_argument("--qbatch", type=int, default=QBATCH,
+                    help="q-sweep members (a smaller batch keeps an ncu capture to a few GB)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.profile and args.profile_leg != "c2":
+        import torch
+        torch.cuda.set_device(0)
+        from initializator_gb300 import build as bt_build
+        bt_build.build()
+        leg = run_qsweep(args, 0) if args.profile_leg == "qsweep" else run_ragged(args, 0)
+        print(json.dumps({"profile_run": True, "leg": args.profile_leg, "value": leg["value"],
+                          "frac": leg["roofline"]["frac"]}))
     else:
         run_ours(args)
 

@@ -92,6 +92,7 @@ struct bt_handle {
     long long mt6_cap = 0;
     std::vector<uint8_t> mask_h;  // host copy of the pore mask (two-component sums)
     uint32_t wait_polls = bt::RING_WAIT_POLLS;  // fast path's plane-ring wait bound
+    int phase_axes = bt::PH_ALL;  // KSPACE: axes with a wave vector somewhere in the schedule
 };
 
 namespace {
@@ -214,6 +215,7 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
         P.fdtt = h->fields_d ? static_cast<const T*>(h->fields_d) : nullptr;
         P.fw = h->fields_d ? static_cast<const T*>(h->fields_d) + 2 * h->comp : nullptr;
         P.wait_polls = h->wait_polls;
+        P.phase_axes = h->phase_axes;
     }
 }
 
@@ -478,6 +480,14 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
     CK(h, cudaMemcpy(h->pulses_d, dp.data(), sizeof(bt::DevPulse) * dp.size(), cudaMemcpyHostToDevice));
     h->steps_h.swap(st);
     h->nsched = nsched;
+    // the axes along which some step's wave vector (at its start or end) is
+    // not zero: the fast path drops the face phases of the others exactly
+    bool kxy = false, kz = false;
+    for (size_t q = 0; q < h->kpos.size(); q += 3) {
+        kxy = kxy || h->kpos[q] != 0.0 || h->kpos[q + 1] != 0.0;
+        kz = kz || h->kpos[q + 2] != 0.0;
+    }
+    h->phase_axes = kxy ? bt::PH_ALL : (kz ? bt::PH_Z : bt::PH_NONE);
     refresh_params(h);
     return BT_OK;
 }

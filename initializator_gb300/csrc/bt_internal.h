@@ -21,6 +21,12 @@ constexpr uint32_t RING_WAIT_POLLS = 1u << 20;
 // relaxation-rate tables (surface relaxation rho/d per solid face).
 constexpr uint8_t CODE_PORE = 64;
 
+// KSPACE fast path: axes whose face phase is not identically 1 over the
+// schedule (StepParams::phase_axes)
+constexpr int PH_NONE = 0;  // no wave vector at any step
+constexpr int PH_Z = 1;     // along z only
+constexpr int PH_ALL = 2;   // any axis
+
 // ghost layer kinds of a domain-face pair (bt_config.boundary)
 constexpr int BC_COPY = 0;
 constexpr int BC_PERIODIC = 1;
@@ -94,6 +100,7 @@ struct StepParams {
     T dtt1[64], dtt2[64];       // dTime * (1/T1), dTime * (1/T2) per face code
     int diffusion;
     int bc[3];                  // ghost layer kind per axis (BC_*)
+    int phase_axes;             // KSPACE: PH_* of the schedule (the fast path's instance)
     int box[6];                 // M(t) trimming box [x0,x1) [y0,y1) [z0,z1)
     double dxd, dyd, dzd, gamma;  // FP64 copies for pulse angles and k phases
     const StepInfo* steps;      // [(nsched + 1) * nbatch], step-major

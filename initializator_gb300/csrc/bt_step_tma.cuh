@@ -180,10 +180,18 @@ static __global__ void cell_velocity_kernel(const StepParams<float> P, float* __
     }
 }
 
-template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK>
+template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK, int PH>
 __global__ void __launch_bounds__(tma::NT, 2)
     step_tma_kernel(const __grid_constant__ StepParams<float> P, const __grid_constant__ TmaMaps M, int first) {
     using namespace tma;
+    // KSPACE: which axes carry a face phase (the schedule's wave vector has a
+    // component along them at some step): every axis (PH_ALL), z alone (PH_Z:
+    // gradients along z only, as every PGSE workload here), or none (PH_NONE:
+    // no gradient); an axis without one uses real face weights, a unit
+    // lab-frame phase and the voxel itself as its copy ghost, which is exact
+    constexpr bool phx = SCHEME == SCHEME_KSPACE && PH == PH_ALL;
+    constexpr bool phz = SCHEME == SCHEME_KSPACE && PH != PH_NONE;
+    constexpr bool ph_axis[3] = {phx, phx, phz};
     using Tl = Tile<TWV>;
     constexpr int TW = Tl::TW, TH = Tl::TH, LW = Tl::LW, RPW = Tl::RPW, SW = Tl::SW, SH = Tl::SH;
     constexpr int OFF_STATE = Tl::OFF_STATE, OFF_U = Tl::OFF_U, OFF_CODE = Tl::OFF_CODE, STAGE = Tl::STAGE;
@@ -306,9 +314,11 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // lab-frame phases (KSPACE), FP64-reduced arguments, each computed once
     // per CTA: the tile's 128 columns by threads 0..127, its 8 rows by threads
     // 128..135, the chunk's planes by the threads from 136 on (wrapping)
-    if constexpr (SCHEME == SCHEME_KSPACE) {
+    if constexpr (phx) {
         if (tid < TW) lab_phase<float>(si->knext[0], x0 + tid, P.dxd, s_ex[tid].x, s_ex[tid].y);
         else if (tid < TW + TH) lab_phase<float>(si->knext[1], y0 + tid - TW, P.dyd, s_ey[tid - TW].x, s_ey[tid - TW].y);
+    }
+    if constexpr (phz) {
         for (int q = (tid + NT - (TW + TH)) % NT; q < z1 - z0; q += NT)
             lab_phase<float>(si->knext[2], z0 + q, P.dzd, s_ez[q].x, s_ez[q].y);
     }
@@ -318,7 +328,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
     if (cta0 && !first) reduce_members<float>(P, P.partials_prev, step - 1, nb_per, red);
     __syncthreads();
     float exr[QX] = {1.f, 1.f, 1.f, 1.f}, exi[QX] = {0.f, 0.f, 0.f, 0.f};
-    if constexpr (SCHEME == SCHEME_KSPACE) {
+    if constexpr (phx) {
 #pragma unroll
         for (int i = 0; i < QX; ++i) {
             const float2 e = s_ex[QX * xl + i];
@@ -334,14 +344,13 @@ __global__ void __launch_bounds__(tma::NT, 2)
         gdy = (float)(si->grad[1] * P.dyd);
         gdz = (float)(si->grad[2] * P.dzd);
     }
-    float ph[3][2];  // exp(+i k d) per axis; the + face uses its conjugate
-    if constexpr (SCHEME == SCHEME_KSPACE) {
+    float ph[3][2] = {{1.f, 0.f}, {1.f, 0.f}, {1.f, 0.f}};  // exp(+i k d) per axis; the + face uses its conjugate
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < 3; ++a)
+        if (ph_axis[a]) {
             ph[a][0] = si->phasef[a][0];
             ph[a][1] = si->phasef[a][1];
         }
-    }
     // summation mask of this thread's 4 voxels (trimming box, inside the grid)
     uint32_t xmask = 0;
 #pragma unroll
@@ -423,8 +432,11 @@ __global__ void __launch_bounds__(tma::NT, 2)
     // in the k frame rotated so that the stencil's face phase (exp(+i th) on
     // the lower face, its conjugate on the upper) brings it back to the voxel
     auto ghost = [&](float& gr, float& gi, float& gz, float mr, float mi, float mz, int a, bool upper) {
-        if constexpr (SCHEME == SCHEME_KSPACE) {
-            const float c = ph[a][0], s = upper ? -ph[a][1] : ph[a][1];
+        if (a == 2 ? phz : phx) {
+            // selected, not indexed: a runtime index would put ph in local memory
+            const float pc = a == 0 ? ph[0][0] : (a == 1 ? ph[1][0] : ph[2][0]);
+            const float ps = a == 0 ? ph[0][1] : (a == 1 ? ph[1][1] : ph[2][1]);
+            const float c = pc, s = upper ? -ps : ps;
             gr = c * mr + s * mi;
             gi = c * mi - s * mr;
         } else {
@@ -626,10 +638,22 @@ __global__ void __launch_bounds__(tma::NT, 2)
                     accr += c * ar - s_ * bi;
                     acci += c * ai + s_ * br;
                 };
+                // an axis without a phase: real weights on both parts
+                auto axis_real = [&](float wm, float wp, float mr, float mi, float pr_, float pi_, float& accr,
+                                     float& acci) {
+                    accr += wm * mr + wp * pr_;
+                    acci += wm * mi + wp * pi_;
+                };
                 float tr = -wsum * px0, ti = -wsum * py0;
-                axis(wxm, wxp, xm[0][i], xm[1][i], xp[0][i], xp[1][i], ph[0][0], ph[0][1], tr, ti);
-                axis(wym, wyp, ym[0][i], ym[1][i], yp[0][i], yp[1][i], ph[1][0], ph[1][1], tr, ti);
-                axis(wzm, wzp, bel[0][i], bel[1][i], abv[0][i], abv[1][i], ph[2][0], ph[2][1], tr, ti);
+                if constexpr (phx) {
+                    axis(wxm, wxp, xm[0][i], xm[1][i], xp[0][i], xp[1][i], ph[0][0], ph[0][1], tr, ti);
+                    axis(wym, wyp, ym[0][i], ym[1][i], yp[0][i], yp[1][i], ph[1][0], ph[1][1], tr, ti);
+                } else {
+                    axis_real(wxm, wxp, xm[0][i], xm[1][i], xp[0][i], xp[1][i], tr, ti);
+                    axis_real(wym, wyp, ym[0][i], ym[1][i], yp[0][i], yp[1][i], tr, ti);
+                }
+                if constexpr (phz) axis(wzm, wzp, bel[0][i], bel[1][i], abv[0][i], abv[1][i], ph[2][0], ph[2][1], tr, ti);
+                else axis_real(wzm, wzp, bel[0][i], bel[1][i], abv[0][i], abv[1][i], tr, ti);
                 ax += tr;
                 ay += ti;
             }
@@ -641,7 +665,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
             o[2][i] = pore ? az : 0.f;
             const bool take = (smask >> i) & 1u;
             const float mr = take ? o[0][i] : 0.f, mi = take ? o[1][i] : 0.f;
-            if constexpr (SCHEME == SCHEME_KSPACE) {
+            if constexpr (phx) {
                 sx_r += exr[i] * mr - exi[i] * mi;
                 sx_i += exr[i] * mi + exi[i] * mr;
             } else {
@@ -650,12 +674,16 @@ __global__ void __launch_bounds__(tma::NT, 2)
             }
             sz_ += take ? o[2][i] : 0.f;
         }
-        if constexpr (SCHEME == SCHEME_KSPACE) {
+        if constexpr (phx) {
             // lab frame: multiply the row sum by exp(-i k_y y) exp(-i k_z z)
             const float2 ey = s_ey[row], ez = s_ez[z - z0];
             const float er = ey.x * ez.x - ey.y * ez.y, ei = ey.x * ez.y + ey.y * ez.x;
             acc[0].add(er * sx_r - ei * sx_i);
             acc[1].add(er * sx_i + ei * sx_r);
+        } else if constexpr (phz) {
+            const float2 ez = s_ez[z - z0];
+            acc[0].add(ez.x * sx_r - ez.y * sx_i);
+            acc[1].add(ez.x * sx_i + ez.y * sx_r);
         } else {
             acc[0].add(sx_r);
             acc[1].add(sx_i);
@@ -752,19 +780,19 @@ static inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, int smem, cud
     return cfg;
 }
 
-template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK = false>
+template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK = false, int PH = PH_ALL>
 static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, bool first, cudaStream_t s) {
     constexpr int smem = tma::Tile<TWV>::SMEM;
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK>,
+        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         configured = true;
     }
     cudaLaunchAttribute attr[1];
     const cudaLaunchConfig_t cfg = pdl_config(grid, dim3(tma::NT), smem, s, attr);
-    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK>, p, m, first ? 1 : 0);
+    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH>, p, m, first ? 1 : 0);
 }
 
 // the fast path's kernels of one tile width
@@ -781,6 +809,15 @@ static cudaError_t launch_step_tma_w(const StepParams<float>& p, const TmaMaps& 
     if (p.bc[0] != BC_COPY || p.bc[1] != BC_COPY || p.bc[2] != BC_COPY) {
         if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, true>(p, m, grid, first, s);
         return launch_tma_t<SCHEME_KSPACE, false, false, TWV, true>(p, m, grid, first, s);
+    }
+    // the phase axes of the schedule (bt_api.cu sets p.phase_axes)
+    if (p.phase_axes == PH_Z) {
+        if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, false, PH_Z>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_Z>(p, m, grid, first, s);
+    }
+    if (p.phase_axes == PH_NONE) {
+        if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, false, PH_NONE>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_NONE>(p, m, grid, first, s);
     }
     if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV>(p, m, grid, first, s);
     return launch_tma_t<SCHEME_KSPACE, false, false, TWV>(p, m, grid, first, s);

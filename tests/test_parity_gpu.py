@@ -271,6 +271,37 @@ def test_tma_path_matches_generic(shape, flow, scheme, btlib, monkeypatch):
     assert rel_err(outs[1][1], outs[0][1]) <= 1e-5
 
 
+@pytest.mark.parametrize("axis", [(0.2, 0.5, 1.0), (0.0, 0.0, 1.0), None])
+@pytest.mark.parametrize("shape", [(20, 12, 100), (18, 40, 60)])
+def test_tma_phase_axes_instances(shape, axis, btlib, monkeypatch):
+    """KSPACE fast path picks its instance from the schedule's wave vectors: a
+    gradient with x/y components (every face phase), along z only (z phase,
+    real x/y weights), none (no phase). Each against the generic FP32 kernel:
+    fields and M(t) within 1e-5; with a refocusing pulse so the pulse step's
+    generic launch and the fast steps around it share the field."""
+    import initializator_gb300 as bt
+    mask, vel, st0, kw = _random_case(shape, seed=71 + sum(shape), flow=True)
+    kw.update(main_field=(0, 0, 1), vector_mult=0, gamma=bt.GAMMA_PROTON, grad=(0.0, 0.0, 0.0))
+    n = 90
+    wave = None if axis is None else bt.kspace_waveform_pgse(n, kw["dt"], 0.08, 8 * kw["dt"], 40 * kw["dt"],
+                                                               axis=axis)
+    rf = [(bt.pgse_refocus_step(kw["dt"], 40 * kw["dt"]), 2, math.pi, (1.0, 0.0, 0.0))]
+    outs = []
+    for no_tma in ("1", None):
+        if no_tma:
+            monkeypatch.setenv("BT_NO_TMA", no_tma)
+        else:
+            monkeypatch.delenv("BT_NO_TMA", raising=False)
+        with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, scheme=bt.BT_SCHEME_KSPACE, **kw)) as s:
+            s.upload_geometry(mask, vel)
+            s.set_schedule(rf, grad_wave=wave)
+            s.set_state(st0)
+            mt = s.run(n)
+            outs.append((s.get_state(), mt))
+    assert rel_err(outs[1][0], outs[0][0]) <= 1e-5
+    assert rel_err(outs[1][1], outs[0][1]) <= 1e-5
+
+
 def test_tma_zsplits_and_autotune(btlib, monkeypatch):
     """Any z-chunking of the fast path gives the same field (chunks never come
     out empty: 38 chunks of 256 planes would leave the last one empty without
