@@ -269,7 +269,8 @@ long long bt_launch_count(const bt_handle* h);
  * ordered on one stream are independent, but calls that overlap on the GPU
  * race and must not be issued. The first call on a device (and the first
  * after its context was reset) looks up the array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture. Grids
+ * (cudaGetSymbolAddress) and must come before any stream capture: made while
+ * `stream` is capturing, it returns BT_E_ARG (message on stderr). Grids
  * above BT_NOALLOC_MAX_VOXELS voxels or
  * BT_NOALLOC_MAX_BLOCKS blocks return BT_E_SIZE (with a message on stderr).
  * A NaN/Inf field shows as non-finite sums (no watchdog status here). */

@@ -85,7 +85,10 @@ unsigned long long current_context_id() {
 // host-side name of a __device__ array is only a stand-in; the address a
 // kernel may use comes from cudaGetSymbolAddress (which also creates the
 // device's context on a first call).
-cudaError_t scratch_for_current_device(unsigned char** out) {
+// The look-up is not a stream operation; a call whose look-up would fall
+// inside a stream capture is refused (cudaErrorStreamCaptureUnsupported), so
+// the rule that the first call on a device precedes any capture is enforced.
+cudaError_t scratch_for_current_device(cudaStream_t stream, unsigned char** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -93,6 +96,9 @@ cudaError_t scratch_for_current_device(unsigned char** out) {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     const unsigned long long ctx = current_context_id();
     if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+            return cudaErrorStreamCaptureUnsupported;
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
@@ -242,8 +248,15 @@ extern "C" int bt_step_noalloc(const bt_config* cfg, const uint8_t* mask, const 
     }
     const dim3 grid(gx, gy, zsplit);
     unsigned char* scratch = nullptr;
-    if (scratch_for_current_device(&scratch) != cudaSuccess) return BT_E_CUDA;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const cudaError_t se = scratch_for_current_device(s, &scratch);
+    if (se == cudaErrorStreamCaptureUnsupported) {
+        std::fprintf(stderr,
+                     "bt_step_noalloc: the first call on a device looks up its scratch array and must come before "
+                     "any stream capture\n");
+        return BT_E_ARG;
+    }
+    if (se != cudaSuccess) return BT_E_CUDA;
     // the run-control block must start at zero (step 0, no ticket, no status)
     if (cudaMemsetAsync(scratch + OFF_CTL, 0, sizeof(bt::Ctl), s) != cudaSuccess) return BT_E_CUDA;
     noalloc_step_record_kernel<<<1, 32, 0, s>>>(reinterpret_cast<bt::StepInfo*>(scratch + OFF_STEP),
