@@ -47,7 +47,9 @@ extern "C" {
  *   advection and diffusion stencil, but the gradient precession
  *   exp(-i*gamma*(G.r)*dt) is exact: the transverse field is carried in the
  *   frame of the wave vector k(t) = gamma * int G dt, accumulated in FP64 on
- *   the host, and enters the stencil as per-step face phase factors.
+ *   the host, and enters the stencil as per-step face phase factors taken
+ *   at the middle of the step (half the step's precession, the stencil, the
+ *   other half: second order in dt for the gradient dephasing).
  *   Fields passed in and out are always in the lab frame. */
 /* BT_SCHEME_MACCORMACK: the reference's GPU scheme (solve_gpu's
  *   ExplicitMakUpgrade, src/NmrRelaxationSolveKernels.cu:637-967,1473-1498):

@@ -444,9 +444,18 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
             if (s == nsched)  // the default entry used beyond the table: cfg gradient, no pulses
                 for (int a = 0; a < 3; ++a) si.grad[a] = c.grad[a];
             for (int a = 0; a < 3; ++a) h->kpos[3 * (s * nb + b) + a] = k[a];
+            // KSPACE: the stencil acts at the middle of the step (half the
+            // step's precession, the stencil, the other half): a precession
+            // only moves the frame and leaves the stored values alone, so this
+            // symmetric split costs nothing but taking the face phases at
+            // k + gamma G dt / 2, and makes the gradient dephasing of the step
+            // second order in dt (the k at its start would make it first order)
+            double km[3] = {k[0], k[1], k[2]};
+            if (c.scheme == BT_SCHEME_KSPACE && s < nsched)
+                for (int a = 0; a < 3; ++a) km[a] = k[a] + 0.5 * (c.gamma * si.grad[a] * c.dt);
             for (int a = 0; a < 3; ++a) {
                 // neighbour at -d: exp(+i k d); at +d: exp(-i k d)
-                const double ang = k[a] * d3[a];
+                const double ang = km[a] * d3[a];
                 si.phase[2 * a][0] = std::cos(ang);
                 si.phase[2 * a][1] = std::sin(ang);
                 si.phase[2 * a + 1][0] = std::cos(ang);
@@ -456,7 +465,7 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
                 // periodic faces: exp(-i k_a n_a d_a), the far edge cell's
                 // k-frame value moved across the period
                 const int n3[3] = {c.nx, c.ny, c.nz};
-                const double wa = k[a] * ((double)n3[a] * d3[a]);
+                const double wa = km[a] * ((double)n3[a] * d3[a]);
                 si.wrap[a][0] = std::cos(wa);
                 si.wrap[a][1] = -std::sin(wa);
                 si.wrapf[a][0] = (float)si.wrap[a][0];

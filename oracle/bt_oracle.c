@@ -447,10 +447,11 @@ static void add_impulse(const bto_params* p, ofields_t* f, const bto_pulse* pu) 
 
 /* Physics mode (no reference counterpart): B0 along z, the gradient field
  * B_z(r) = G.r with r = (c + 0.5) * d turns the transverse magnetization by
- * exp(-i * gamma * B_z * dt) over the step, applied exactly after the explicit
- * relaxation/advection/diffusion update (dM/dt = gamma M x B, as the
- * reference's cross product, but integrated exactly). */
-static void precess_exact(const bto_params* p, ofields_t* f, const double G[3]) {
+ * exp(-i * gamma * B_z * frac * dt) (dM/dt = gamma M x B, as the reference's
+ * cross product, but integrated exactly); a step applies half of its turn
+ * before the explicit relaxation/advection/diffusion update and half after
+ * (a symmetric split, second order in dt for the gradient dephasing). */
+static void precess_exact(const bto_params* p, ofields_t* f, const double G[3], double frac) {
     const grid_t* g = &f->g;
     #pragma omp parallel for schedule(static)
     for (int k = 1; k <= g->nz; k++)
@@ -460,7 +461,7 @@ static void precess_exact(const bto_params* p, ofields_t* f, const double G[3]) 
                 if (f->act[c] != 1) continue;
                 double bz = G[0] * (((double)i - 0.5) * p->dx) + G[1] * (((double)j - 0.5) * p->dy)
                           + G[2] * (((double)k - 0.5) * p->dz);
-                double th = p->gamma * bz * p->dt;
+                double th = p->gamma * bz * (frac * p->dt);
                 double cs = cos(th), sn = sin(th);
                 double x = f->mx[c], y = f->my[c];
                 f->mx[c] = x * cs + y * sn;
@@ -559,6 +560,15 @@ static int run_impl(const bto_params* p, const uint8_t* mask,
     for (long long s = 0; s < nsteps; s++) {
         double G[3] = {p->grad[0], p->grad[1], p->grad[2]};
         if (grad_wave) { G[0] = grad_wave[3 * s]; G[1] = grad_wave[3 * s + 1]; G[2] = grad_wave[3 * s + 2]; }
+        if (p->vector_mult == 2) {
+            /* physics mode: half the step's precession before the update, half
+             * after (a symmetric split), ghosts of the turned field first: copies
+             * in the first step (the initial layer), the run's kind afterwards */
+            static const int copy_layers[3] = {0, 0, 0};
+            const int* bm = s == 0 ? copy_layers : p->boundary;
+            precess_exact(p, &f, G, 0.5);
+            bc_apply_d(g, f.mx, bm); bc_apply_d(g, f.my, bm); bc_apply_d(g, f.mz, bm);
+        }
         if (maccormack) {
             /* predictor into the add arrays (zero in solid), copy ghosts, then
              * the corrector from it into P's partner; M = the corrected field */
@@ -585,7 +595,7 @@ static int run_impl(const bto_params* p, const uint8_t* mask,
                 memcpy(&f.my[c0], &f.ay[c0], sizeof(double) * g->nx);
                 memcpy(&f.mz[c0], &f.az[c0], sizeof(double) * g->nx);
             }
-        if (p->vector_mult == 2) precess_exact(p, &f, G);
+        if (p->vector_mult == 2) precess_exact(p, &f, G, 0.5);
         for (int q = 0; q < npulses; q++)
             if (pulses[q].step == s) add_impulse(p, &f, &pulses[q]);
         bc_apply_d(g, f.mx, p->boundary); bc_apply_d(g, f.my, p->boundary); bc_apply_d(g, f.mz, p->boundary);

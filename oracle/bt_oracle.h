@@ -32,7 +32,8 @@ typedef struct {
     double p_eq;             /* equilibriumMagnetization */
     int vector_mult;         /* nVectorMult: 1 = reference Euler cross product M x B_noise;
                                 2 = exact precession about z by gamma*(G.r)*dt (physics
-                                mode, B0 along z; r = (c + 0.5) * d) */
+                                mode, B0 along z; r = (c + 0.5) * d), half of it before
+                                the update and half after */
     int velocity;            /* nVelocity */
     int diffusion;           /* nDiffusion */
     int buffer[3];           /* bufferX/Y/Z trimming of the M(t) sums */
