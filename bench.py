@@ -552,6 +552,48 @@ def run_compat(args, lr):
     return out
 
 
+LEARNED_WEIGHTS = os.path.join(ROOT, "initializator_gb300", "data", "rate_closure_g0.npz")
+LEARNED_CASES = [((64, 64, 64), 88, "sphere", 900, 0.0), ((64, 64, 64), 88, "grf", 901, 0.0),
+                 ((256, 256, 256), 250, "sphere", 902, 0.0), ((64, 64, 64), 88, "sphere", 900, 0.2)]
+
+
+def run_learned(args, lr):
+    """The learned coarse relaxation closure (initializator_gb300/rate_closure.py,
+    weights trained by `python -m initializator_gb300.rate_closure --save`):
+    on held-out seeded cases drawn like its training samples (sphere packs r 6
+    with 35 % solid, Gaussian random fields, flow 1 mm/s, rho 10 um/s), the
+    M(t) error against the FP64 fine solve of the fine FP32 solve, the plain
+    coarse solve (2 dx, 4 dt) and the learned one, and the time to the M(t)
+    curve of the fine FP32 solve and of the learned one (network + coarse
+    solve). Without a gradient (what it was trained on) and, for the record,
+    under PGSE at 0.2 T/m, where the coarse geometry's diffusion error is
+    not corrected."""
+    import torch
+
+    from initializator_gb300 import closure as C
+    from initializator_gb300 import rate_closure as R
+    if not os.path.exists(LEARNED_WEIGHTS):
+        return {"unavailable": "no trained weights at initializator_gb300/data/rate_closure_g0.npz"}
+    clo = R.RateClosure.load(LEARNED_WEIGHTS, device=f"cuda:{lr}")
+    rows = []
+    for shape, n_coarse, kind, seed, g in LEARNED_CASES:
+        case = C.Case.pgse(shape, seed=seed, kind=kind, g_amp=g, n_coarse=n_coarse, device=f"cuda:{lr}")
+        rc = R.RateCase(case, n_coarse)
+        ref = case.reference_mt(n_coarse)
+        plain, _ = rc.rollout(None)
+        R.time_to_mt(rc, clo)  # warm-up
+        t_fine, t_learned, fine, learned = R.time_to_mt(rc, clo)
+        rows.append({"grid": list(shape), "fine_steps": 4 * n_coarse, "geometry": kind, "seed": seed, "G": g,
+                     "err_fine_f32": R.mt_error(fine, ref), "err_plain_coarse": R.mt_error(plain, ref),
+                     "err_learned": R.mt_error(learned, ref), "s_fine_f32": t_fine, "s_learned": t_learned,
+                     "speedup": t_fine / t_learned})
+        del case, rc
+        torch.cuda.empty_cache()
+    return {"definition": "err = max_t |M_xy(t) - M_xy,FP64 fine(t)| / |M_xy(first)|; time to M(t) after the "
+                          "geometry is known (handle, upload, steps; the learned form adds the network)",
+            "weights": os.path.relpath(LEARNED_WEIGHTS, ROOT), "cases": rows}
+
+
 def run_reference(args):
     r, w, _ = rank_info()
     if r != 0:
@@ -684,6 +726,7 @@ def run_ours(args):
     c5 = None if args.no_c5 else run_c5(args, lr)
     c1 = run_c1(args, lr) if args.c1 else None
     compat = None if args.no_compat else run_compat(args, lr)
+    learned = None if args.no_learned else run_learned(args, lr)
 
     out = None
     if r == 0:
@@ -710,6 +753,7 @@ def run_ours(args):
             "c5": c5,
             "c1": c1,
             "compat_f64": compat,
+            "learned": learned,
         }
         print(json.dumps(out))
     if w > 1:
@@ -728,6 +772,8 @@ def main():
     ap.add_argument("--no-qsweep", action="store_true", help="skip the batched 32-gradient q-sweep (C3a) leg")
     ap.add_argument("--no-ragged", action="store_true", help="skip the 48-sample ragged batch (C3b) leg")
     ap.add_argument("--no-c5", action="store_true", help="skip the 1024x1024x768 (C5, ~100 GB with its FP64 check) leg")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned coarse closure leg (error and time to M(t) on held-out cases)")
     ap.add_argument("--no-compat", action="store_true",
                     help="skip the MacCormack FP64 (the reference's GPU scheme) leg at C1 and C2")
     ap.add_argument("--no-f64-check", action="store_true",
