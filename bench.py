@@ -582,15 +582,17 @@ def run_learned(args, lr):
         ref = case.reference_mt(n_coarse)
         plain, _ = rc.rollout(None)
         R.time_to_mt(rc, clo)  # warm-up
-        t_fine, t_learned, fine, learned = R.time_to_mt(rc, clo)
+        t, fine, learned = R.time_to_mt(rc, clo)
         rows.append({"grid": list(shape), "fine_steps": 4 * n_coarse, "geometry": kind, "seed": seed, "G": g,
                      "err_fine_f32": R.mt_error(fine, ref), "err_plain_coarse": R.mt_error(plain, ref),
-                     "err_learned": R.mt_error(learned, ref), "s_fine_f32": t_fine, "s_learned": t_learned,
-                     "speedup": t_fine / t_learned})
+                     "err_learned": R.mt_error(learned, ref), **t,
+                     "speedup": t["s_fine"] / t["s_learned"],
+                     "speedup_steps": t["s_fine_steps"] / t["s_learned_steps"]})
         del case, rc
         torch.cuda.empty_cache()
     return {"definition": "err = max_t |M_xy(t) - M_xy,FP64 fine(t)| / |M_xy(first)|; time to M(t) after the "
-                          "geometry is known (handle, upload, steps; the learned form adds the network)",
+                          "geometry is known (handle, upload, steps; the learned form adds the network); "
+                          "*_steps: device time of the steps (and the network) alone",
             "weights": os.path.relpath(LEARNED_WEIGHTS, ROOT), "cases": rows}
 
 

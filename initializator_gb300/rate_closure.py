@@ -255,26 +255,50 @@ def mt_error(mt, ref):
     return C.mt_error(mt, ref)
 
 
+def _timed_run(s, nsteps):
+    """M(t) of nsteps steps of handle s and the device time of the steps
+    alone (CUDA events on the handle's stream)."""
+    import torch
+    st = s.torch_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    s.run_async(nsteps)
+    e1.record(st)
+    s.synchronize()
+    return s.read_mt(nsteps), e0.elapsed_time(e1) / 1e3
+
+
 def time_to_mt(rc: RateCase, clo: RateClosure):
-    """Seconds to the M(t) curve of the sample, everything after the
-    geometry is known: the fine FP32 solve (handle, upload, 4 n fine steps)
-    and the learned coarse solve (network, handle with per-voxel rates, n
-    coarse steps). Returns (fine s, learned s, fine M(t), learned M(t))."""
+    """Time to the M(t) curve of the sample once its geometry is known: the
+    fine FP32 solve (handle, upload, 4 n fine steps) and the learned coarse
+    solve (network, handle with per-voxel rates, n coarse steps). Returns
+    {s_fine, s_learned: wall seconds of everything; s_fine_steps,
+    s_learned_steps: device seconds of the steps (and the network)}, fine
+    M(t), learned M(t)."""
     import time
 
     import torch
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     s = rc.case.solver(0)
-    fine = s.run(4 * rc.n)[3::4]
+    fine, t_fs = _timed_run(s, 4 * rc.n)
+    fine = fine[3::4]
     s.close()
     t_fine = time.perf_counter() - t0
     t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
     with torch.no_grad():
         corr, _, _ = clo.predict([rc])
-    mt, _ = rc.rollout(corr[0].double().cpu().numpy())
+    e1.record()
+    torch.cuda.synchronize()
+    t_net = e0.elapsed_time(e1) / 1e3
+    cs = rc.solver(corr[0].double().cpu().numpy())
+    mt, t_cs = _timed_run(cs, rc.n)
+    cs.close()
     t_learned = time.perf_counter() - t0
-    return t_fine, t_learned, fine, mt
+    return ({"s_fine": t_fine, "s_learned": t_learned, "s_fine_steps": t_fs, "s_learned_steps": t_net + t_cs},
+            fine, 8.0 * mt)
 
 
 def evaluate(shape=(64, 64, 64), n_coarse=88, n_train=8, outer=5, inner=120, g_test=0.2, seed=5, g_train=0.0,
@@ -311,9 +335,9 @@ def evaluate(shape=(64, 64, 64), n_coarse=88, n_train=8, outer=5, inner=120, g_t
         f32 = case.reference_mt(n_coarse, precision=0)
         plain, _ = rc.rollout(None)
         time_to_mt(rc, clo)  # warm-up: kernels loaded, graphs captured
-        t_fine, t_learned, _, corr_mt = time_to_mt(rc, clo)
+        times, _, corr_mt = time_to_mt(rc, clo)
         row = {"case": kind, "G": g, "err_fine_f32": mt_error(f32, ref), "err_plain": mt_error(plain, ref),
-               "err_closure": mt_error(corr_mt, ref), "s_fine": t_fine, "s_learned": t_learned}
+               "err_closure": mt_error(corr_mt, ref), **times}
         out["held_out"].append(row)
         if log:
             log(row)
