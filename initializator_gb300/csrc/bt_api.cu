@@ -992,9 +992,11 @@ int bt_run_many(bt_handle* const* hs, int n, long long nsteps) {
     for (int i = 0; i < n; ++i)
         if (!hs[i]) return BT_E_ARG;
     // the handles share the GPU: their fast paths get z-chunks such that all
-    // of them together launch about four waves of two CTAs per SM, each
+    // of them together launch about two waves of two CTAs per SM, each
     // handle's share in proportion to its voxels (a handle alone would take
-    // four waves by itself, and many short chunks pay many CTA prologues)
+    // four waves by itself, and many short chunks pay many CTA prologues;
+    // 48 samples of 48..192 voxels a side: 2 waves 0.599 of the roofline,
+    // 3 waves 0.597, 4 waves 0.588, 6 waves 0.593)
     if (n > 1) {
         long long vox_all = 0;
         for (int i = 0; i < n; ++i)
@@ -1005,7 +1007,7 @@ int bt_run_many(bt_handle* const* hs, int n, long long nsteps) {
             const bt_config& c = h->cfg;
             const int tw = h->ttx, th = bt::tile_rows(tw);
             const double tiles = (double)((c.nx + tw - 1) / tw) * ((c.ny + th - 1) / th) * h->nb;
-            const double want = 8.0 * h->num_sms * ((double)h->nvox * h->nb / (double)vox_all) / tiles;
+            const double want = 4.0 * h->num_sms * ((double)h->nvox * h->nb / (double)vox_all) / tiles;
             const int zs = (int)std::max(1.0, std::min(std::floor(want + 0.5), (double)std::max(1, c.nz / 8)));
             if (zs != h->tzsplit) {
                 CK(h, cudaStreamSynchronize(h->stream));
@@ -1237,13 +1239,16 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
         if (best_zsplit) *best_zsplit = h->gzsplit;
         return BT_OK;
     }
-    // candidate z-splits: waves of 2 CTAs per SM from 1 to 8, chunks of >= 4 planes
+    // candidate z-splits: for 1 to 8 waves of 2 CTAs per SM, the split whose
+    // CTAs just fill that many waves (its last wave full or nearly so) and the
+    // one just above (a last wave barely started); chunks of >= 4 planes
     const bt_config& c = h->cfg;
     const long long tiles = (long long)h->tgrid.y * h->tgrid.z * h->nb;
     std::vector<int> cand;
     for (int waves = 1; waves <= 8; ++waves) {
-        const long long zs = (waves * 2LL * h->num_sms + tiles - 1) / tiles;
-        if (zs >= 1 && zs <= std::max(1, c.nz / 4)) cand.push_back((int)zs);
+        const long long below = waves * 2LL * h->num_sms / tiles;
+        for (long long zs : {below, below + 1})
+            if (zs >= 1 && zs <= std::max(1, c.nz / 4)) cand.push_back((int)zs);
     }
     cand.push_back(default_tma_split(h));
     std::sort(cand.begin(), cand.end());

@@ -90,7 +90,7 @@ struct Tile {
     static constexpr int STAGE = (OFF_CODE + SZ_CODE + 127) / 128 * 128;
     static constexpr int OFF_AUX = NSTAGE * STAGE;  // tables, barriers, reduction
     // aux layout (bytes from OFF_AUX)
-    static constexpr int AUX_TAB = 0;                     // 128 rows: 6 face weights, dt/T1, dt/T2, 4 unused
+    static constexpr int AUX_TAB = 0;                     // 128 rows: 6 face weights, dt/T1, dt/T2, their sum, 3 unused
     static constexpr int AUX_EY = AUX_TAB + 128 * TAB_ROW * 4;  // exp(-i k_y y), TH float2
     static constexpr int AUX_BARS = AUX_EY + (8 * TH + 63) / 64 * 64;  // full[NSTAGE], empty[NSTAGE]
     static constexpr int AUX_FLAGS = AUX_BARS + 64;
@@ -272,7 +272,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
         s_flags[0] = 0;
     }
     // per-CTA table indexed by the voxel code (bit 6 pore, bits 0-5 solid
-    // faces): six face diffusion weights, dt/T1, dt/T2; all zero for solid.
+    // faces): six face diffusion weights, dt/T1, dt/T2, the weights' sum; all
+    // zero for solid.
     // It depends on the launch's parameters only, so with programmatic
     // dependent launch it is built while the previous step still runs.
     if (tid < 128) {
@@ -285,6 +286,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
                                      dm * ((f & 8) ? sy : ky));
         s_tab[3 * tid + 1] = make_float4(dm * ((f & 16) ? sz : kz), dm * ((f & 32) ? sz : kz),
                                          pore ? P.dtt1[f] : 0.f, pore ? P.dtt2[f] : 0.f);
+        // the six diffusion weights' sum, added in the order the voxel loop
+        // used to add them
+        const float4 a = s_tab[3 * tid], c = s_tab[3 * tid + 1];
+        s_tab[3 * tid + 2] = make_float4(((a.x + a.y) + (a.z + a.w)) + (c.x + c.y), 0.f, 0.f, 0.f);
     }
     // everything below reads what the previous step wrote (the field, the
     // step counter): wait until that grid has completed and its writes are
@@ -604,7 +609,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
                 wzp -= fminf(uz[i], 0.f);
                 wzm += fmaxf(uz[i], 0.f);
             }
-            const float wsum = ((wxm + wxp) + (wym + wyp)) + (wzm + wzp);
+            // the sum of the six face weights: the diffusion part from the
+            // table; upwind adds max(u, 0) - min(u, 0) = |u| per axis
+            float wsum = reinterpret_cast<const float*>(s_tab + 3 * cd + 2)[0];
+            if constexpr (VEL) wsum = ((wsum + fabsf(ux[i])) + fabsf(uy[i])) + fabsf(uz[i]);
             const float px0 = cur[0][i], py0 = cur[1][i], pz0 = cur[2][i];
             float ax, ay, az;
             if constexpr (SCHEME == SCHEME_REF) {

@@ -343,7 +343,7 @@ def test_tma_zsplits_and_autotune(btlib, monkeypatch):
 
 def test_ragged_shared_chunking(btlib):
     """run_many gives handles that share the GPU longer z-chunks than each
-    would take alone (here 5 instead of 8 per column for eight 256 x 128 x 64
+    would take alone (here 2 instead of 8 per column for eight 256 x 128 x 64
     grids); fields stay bit-identical to each handle run alone and M(t) agrees
     to 1e-6 (only the FP32 grouping of the per-thread sums changes)."""
     import initializator_gb300 as bt
