@@ -212,17 +212,25 @@ void* bt_stream(bt_handle* h);
 int bt_measure(bt_handle* h, double* sums3);
 
 /* Pick the z-chunking of the FP32 fast path by timing trial_steps steps for
- * each candidate split (no reference counterpart: the reference launches one
- * thread per voxel, cu:1475-1476). The field and step index are restored.
- * *best_zsplit (may be NULL) receives the chosen split. */
-int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit);
+ * each candidate (no reference counterpart: the reference launches one
+ * thread per voxel, cu:1475-1476): for one to eight waves of CTAs, the chunk
+ * count that fills exactly that many waves and the even splits around it.
+ * The field and step index are restored. *best_chunks (may be NULL) receives
+ * the chosen number of chunks per field (as for bt_set_tma_chunks). */
+int bt_autotune(bt_handle* h, int trial_steps, int* best_chunks);
 
 /* The FP32 fast path's z-chunking: zsplit chunks per column (<= 0: the
  * default for a handle running alone, about four waves of CTAs). A no-op for
  * handles without the fast path. bt_run_many sets the chunking of its handles
- * for sharing the GPU (about four waves over all of them together); this call
+ * for sharing the GPU (about two waves over all of them together); this call
  * (or bt_autotune) sets it back for running alone. */
 int bt_set_tma_split(bt_handle* h, int zsplit);
+/* The FP32 fast path's z-chunking as a number of chunks per field in total:
+ * the tile columns get chunks/tiles or one more (so any count of CTAs, e.g.
+ * exactly two waves, can be launched), clamped to at least one chunk per
+ * column and chunks of 1..1024 planes; <= 0: the default. A no-op for handles
+ * without the fast path. */
+int bt_set_tma_chunks(bt_handle* h, int chunks);
 
 /* Failure injection for tests (no reference counterpart): the FP32 fast
  * path's plane-ring waits (mbarrier polls for a plane's TMA copy, and the

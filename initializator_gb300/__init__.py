@@ -71,7 +71,7 @@ EXPORTS = [
     "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
     "bt_run_many", "bt_read_mt", "bt_synchronize", "bt_upload_rates", "bt_set_phase_weights",
     "bt_read_mt_phases", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
-    "bt_version", "bt_autotune", "bt_set_tma_split", "bt_step_noalloc",
+    "bt_version", "bt_autotune", "bt_set_tma_split", "bt_set_tma_chunks", "bt_step_noalloc",
     "bt_conv3d_margin", "bt_conv3d", "bt_conv3d_weight_grad", "bt_conv3d_wgrad_scratch", "bt_conv3d_pack_weights",
     "bt_adamw", "bt_umma_selftest", "bt_field_device", "bt_set_wait_polls",
 ]
@@ -116,6 +116,7 @@ def lib():
         "bt_version": ([], ctypes.c_char_p),
         "bt_autotune": ([vp, i, ctypes.POINTER(ctypes.c_int)], i),
         "bt_set_tma_split": ([vp, i], i),
+        "bt_set_tma_chunks": ([vp, i], i),
         "bt_set_wait_polls": ([vp, ll], i),
         "bt_step_noalloc": ([ctypes.POINTER(Config), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
         "bt_conv3d_margin": ([i, i], ll),
@@ -336,7 +337,8 @@ class Solver:
         return out[0] if self.batch == 1 else out
 
     def autotune(self, trial_steps=64):
-        """Time the candidate z-splits of the FP32 fast path; returns the chosen one."""
+        """Time the candidate z-chunkings of the FP32 fast path; returns the
+        chosen number of chunks per field (see set_chunks)."""
         best = ctypes.c_int(0)
         self._check(self._l.bt_autotune(self._h, int(trial_steps), ctypes.byref(best)), "autotune")
         return best.value
@@ -345,6 +347,11 @@ class Solver:
         """The FP32 fast path's z-chunks per column (0: the default for running
         alone; run_many sets them for sharing the GPU)."""
         self._check(self._l.bt_set_tma_split(self._h, int(zsplit)), "set_tma_split")
+
+    def set_chunks(self, chunks=0):
+        """The FP32 fast path's z-chunks per field in total, spread over the
+        tile columns (they differ by at most one); 0: the default."""
+        self._check(self._l.bt_set_tma_chunks(self._h, int(chunks)), "set_tma_chunks")
 
     def set_wait_polls(self, polls=-1):
         """Failure injection: the fast path's plane-ring waits give up after

@@ -42,7 +42,8 @@ struct bt_handle {
     size_t comp = 0;              // elements per component (pitch*ny*nz)
     int nb = 1;                   // fields advanced together (batch members)
     int gzsplit = 1;              // z-chunks per field, generic kernel
-    int tzsplit = 1;              // z-chunks per field, TMA kernel
+    int tzsplit = 1;              // z-chunks per tile column (at most), TMA kernel
+    int tzlong = 0;               // tile columns with tzsplit chunks (the rest tzsplit - 1)
     int ttx = 128;                // tile width of the TMA kernel (128, or 64 for narrow grids)
     void* state_base[2] = {};     // one allocation per ping-pong side: [batch][component][z][y][pitch]
     void* state[2][3] = {};
@@ -139,7 +140,7 @@ __global__ void code_kernel(const uint8_t* mask, uint8_t* code, int nx, int ny, 
 }
 
 template <typename T>
-void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
+void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit, int zlong = 1 << 30) {
     const bt_config& c = h->cfg;
     const double dTime = c.dt;
     const double Bx = c.main_field[0], By = c.main_field[1], Bz = c.main_field[2];
@@ -158,6 +159,7 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit) {
         P.pitch = h->pitch; P.vxpitch = h->vxpitch; P.cpitch = h->cpitch;
         P.plane = (long long)h->pitch * c.ny;
         P.zsplit = zsplit;
+        P.zlong = zlong;
         P.zchunk = (c.nz + P.zsplit - 1) / P.zsplit;
         P.nbatch = h->nb;
         P.bstride = 3LL * (long long)h->comp;
@@ -224,7 +226,7 @@ void refresh_params(bt_handle* h) {
         fill_params<double>(h, h->pd, h->gzsplit);
     } else {
         fill_params<float>(h, h->pf, h->gzsplit);
-        fill_params<float>(h, h->pt, h->tzsplit);
+        fill_params<float>(h, h->pt, h->tzsplit, h->tzlong);
         // the fast path keeps one partials buffer per input side: a step's
         // partials are read by the next step, which writes the other buffer
         for (int s = 0; s < 2; ++s) {
@@ -296,15 +298,30 @@ int normalise_split(int nz, int zsplit) {
     return (nz + zchunk - 1) / zchunk;
 }
 
-int set_tma_split(bt_handle* h, int zsplit) {
+// tile columns of one field on the fast path
+long long tma_tiles(const bt_handle* h) {
     const bt_config& c = h->cfg;
-    zsplit = normalise_split(c.nz, zsplit);
+    const int tw = h->ttx, th = bt::tile_rows(tw);
+    return (long long)((c.nx + tw - 1) / tw) * ((c.ny + th - 1) / th);
+}
+
+// the fast path's z-chunking: `chunks` chunks per field in total, spread over
+// the tile columns so that they differ by at most one (at least one chunk per
+// column, at most one plane per chunk, chunks of at most 1024 planes)
+int set_tma_chunks(bt_handle* h, long long chunks) {
+    const bt_config& c = h->cfg;
+    const long long tiles = tma_tiles(h);
+    const long long lo = tiles * ((c.nz + 1023) / 1024), hi = tiles * c.nz;
+    chunks = std::max(lo, std::min(hi, chunks));
+    const long long q = chunks / tiles, r = chunks % tiles;
+    const int zsplit = (int)(r ? q + 1 : q), zlong = (int)(r ? r : tiles);
     // unchanged since the last call (tpart is only ever set here): keep the
     // captured graphs
-    if (zsplit == h->tzsplit && h->tpart > 0) return BT_OK;
+    if (zsplit == h->tzsplit && zlong == h->tzlong && h->tpart > 0) return BT_OK;
     const int tw = h->ttx, th = bt::tile_rows(tw);
     const int gx = (c.nx + tw - 1) / tw, gy = (c.ny + th - 1) / th;
     h->tzsplit = zsplit;
+    h->tzlong = zlong;
     h->tgrid = dim3(zsplit * h->nb, gx, gy);
     h->tpart = 3 * (size_t)zsplit * gx * gy * h->nb;
     const size_t need = 2 * h->tpart;
@@ -317,6 +334,11 @@ int set_tma_split(bt_handle* h, int zsplit) {
     }
     refresh_params(h);
     return BT_OK;
+}
+
+// the same number of chunks in every tile column
+int set_tma_split(bt_handle* h, int zsplit) {
+    return set_tma_chunks(h, (long long)normalise_split(h->cfg.nz, zsplit) * tma_tiles(h));
 }
 
 // default split: about 4 waves of 2 CTAs per SM, chunks of at least 8 planes
@@ -1006,12 +1028,13 @@ int bt_run_many(bt_handle* const* hs, int n, long long nsteps) {
             if (!h->use_tma) continue;
             const bt_config& c = h->cfg;
             const int tw = h->ttx, th = bt::tile_rows(tw);
-            const double tiles = (double)((c.nx + tw - 1) / tw) * ((c.ny + th - 1) / th) * h->nb;
-            const double want = 4.0 * h->num_sms * ((double)h->nvox * h->nb / (double)vox_all) / tiles;
-            const int zs = (int)std::max(1.0, std::min(std::floor(want + 0.5), (double)std::max(1, c.nz / 8)));
-            if (zs != h->tzsplit) {
+            const double tiles = (double)((c.nx + tw - 1) / tw) * ((c.ny + th - 1) / th);
+            // this handle's share of the CTAs, per member, as a chunk count
+            const double want = 4.0 * h->num_sms * ((double)h->nvox / (double)vox_all);
+            const long long ch = (long long)std::max(tiles, std::min(std::floor(want + 0.5), tiles * std::max(1, c.nz / 8)));
+            if (ch != (long long)(h->tzsplit - 1) * tma_tiles(h) + h->tzlong) {
                 CK(h, cudaStreamSynchronize(h->stream));
-                int rc = set_tma_split(h, zs);
+                int rc = set_tma_chunks(h, ch);
                 if (rc) return rc;
             }
         }
@@ -1232,25 +1255,39 @@ int bt_set_tma_split(bt_handle* h, int zsplit) {
     return set_tma_split(h, zsplit > 0 ? zsplit : default_tma_split(h));
 }
 
-int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
+int bt_set_tma_chunks(bt_handle* h, int chunks) {
+    if (!h) return BT_E_ARG;
+    if (h->cfg.precision != BT_F32 || !h->use_tma) return BT_OK;  // no fast path on this handle
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (chunks <= 0) return set_tma_split(h, default_tma_split(h));
+    return set_tma_chunks(h, chunks);
+}
+
+int bt_autotune(bt_handle* h, int trial_steps, int* best_chunks) {
     if (!h || trial_steps <= 0) return fail(h, BT_E_ARG, "bad autotune arguments");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
     if (h->cfg.precision != BT_F32 || !h->use_tma) {
-        if (best_zsplit) *best_zsplit = h->gzsplit;
+        if (best_chunks) *best_chunks = h->gzsplit;
         return BT_OK;
     }
-    // candidate z-splits: for 1 to 8 waves of 2 CTAs per SM, the split whose
-    // CTAs just fill that many waves (its last wave full or nearly so) and the
-    // one just above (a last wave barely started); chunks of >= 4 planes
+    // candidate chunkings (chunks per field): for 1 to 8 waves of 2 CTAs per
+    // SM, the chunk count that fills exactly that many waves (tile columns
+    // differing by one chunk), and the even splits just below and just above
+    // it; chunks of >= 4 planes
     const bt_config& c = h->cfg;
-    const long long tiles = (long long)h->tgrid.y * h->tgrid.z * h->nb;
-    std::vector<int> cand;
+    const long long tiles = tma_tiles(h);
+    const long long slots = 2LL * h->num_sms / h->nb;  // CTA slots per member
+    std::vector<long long> cand;
+    auto add = [&](long long chunks) {
+        if (chunks >= tiles && chunks <= tiles * std::max(1, c.nz / 4)) cand.push_back(chunks);
+    };
     for (int waves = 1; waves <= 8; ++waves) {
-        const long long below = waves * 2LL * h->num_sms / tiles;
-        for (long long zs : {below, below + 1})
-            if (zs >= 1 && zs <= std::max(1, c.nz / 4)) cand.push_back((int)zs);
+        const long long below = waves * slots / tiles;
+        add(waves * slots);
+        add(below * tiles);
+        add((below + 1) * tiles);
     }
-    cand.push_back(default_tma_split(h));
+    cand.push_back((long long)default_tma_split(h) * tiles);
     std::sort(cand.begin(), cand.end());
     cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
     // the trial runs advance the field; the caller's field and step are restored
@@ -1264,13 +1301,12 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    int best_zs = h->tzsplit;
+    long long best_ch = (long long)(h->tzsplit - 1) * tiles + h->tzlong;
     int rc = BT_OK;
-    for (int& zs : cand) zs = normalise_split(c.nz, zs);
     std::sort(cand.begin(), cand.end());
     cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
-    for (int zs : cand) {
-        if ((rc = set_tma_split(h, zs))) break;
+    for (long long ch : cand) {
+        if ((rc = set_tma_chunks(h, ch))) break;
         if ((rc = bt_run_async(h, GRAPH_STEPS))) break;  // warm-up and graph capture
         cudaEventRecord(e0, h->stream);
         if ((rc = bt_run_async(h, trial_steps))) break;
@@ -1281,7 +1317,7 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
         if ((rc = check_ctl(h))) break;
         if (ms < best) {
             best = ms;
-            best_zs = zs;
+            best_ch = ch;
         }
     }
     cudaEventDestroy(e0);
@@ -1291,11 +1327,11 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_zsplit) {
     cudaMemcpy(h->state_base[h->cur], keep, sbytes, cudaMemcpyDeviceToDevice);
     cudaFree(keep);
     if (rc) return rc;
-    rc = set_tma_split(h, best_zs);
+    rc = set_tma_chunks(h, best_ch);
     if (rc) return rc;
     rc = bt_set_step(h, step0);
     if (rc) return rc;
-    if (best_zsplit) *best_zsplit = best_zs;
+    if (best_chunks) *best_chunks = (int)((long long)(h->tzsplit - 1) * tiles + h->tzlong);
     return BT_OK;
 }
 

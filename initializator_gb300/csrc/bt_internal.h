@@ -79,7 +79,8 @@ template <typename T>
 struct StepParams {
     int nx, ny, nz, zchunk;
     int pitch, vxpitch, cpitch;
-    int zsplit;                 // z-chunks per field
+    int zsplit;                 // z-chunks per field (fast path: per tile column, at most)
+    int zlong;                  // fast path: tile columns with zsplit chunks; the rest have zsplit - 1
     int nbatch;                 // fields advanced together (q-sweep); 0 or 1 = one
     long long bstride;          // elements from one batch member's field to the next
     long long plane;            // pitch * ny (state and vz plane stride)

@@ -227,10 +227,13 @@ __global__ void __launch_bounds__(tma::NT, 2)
     const unsigned b = blockIdx.x % nb;
     const int zc = (int)(blockIdx.x / nb);
     const int x0 = blockIdx.y * TW, y0 = blockIdx.z * TH;
-    // even chunks (lengths differ by at most one plane), so the CTAs of the
-    // last wave end together
-    const int z0 = (int)((long long)zc * nz / P.zsplit);
-    const int z1 = (int)((long long)(zc + 1) * nz / P.zsplit);
+    // this tile column's chunks: P.zsplit for the first P.zlong tiles (x
+    // fastest), one fewer for the rest, whose last grid index is then empty;
+    // so any chunk count can fill whole waves. Even chunks within a column
+    // (lengths differ by at most one plane).
+    const int nch = P.zsplit - ((int)(blockIdx.y + gridDim.y * blockIdx.z) >= P.zlong ? 1 : 0);
+    const int z0 = zc < nch ? (int)((long long)zc * nz / nch) : 0;
+    const int z1 = zc < nch ? (int)((long long)(zc + 1) * nz / nch) : 0;
     const int d = (zc & 1) ? -1 : 1;
     const int xb = x0 + QX * xl;  // first of this thread's 4 voxels
     const int y = y0 + row;
@@ -257,8 +260,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
         }
         return pl;
     };
-    // the host never makes an empty chunk; a CTA that still gets one issues
-    // no copy, waits on nothing and contributes zero sums
+    // a CTA without a chunk (the short columns' last grid index) issues no
+    // copy, waits on nothing and contributes zero sums
     const bool empty = z1 <= z0;
     const int nplanes = empty ? 0 : z1 - z0 + 2;
     // plane q lands in slot q % NSTAGE as that slot's (q / NSTAGE)-th phase
