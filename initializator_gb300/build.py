@@ -4,6 +4,7 @@ Translation units are compiled in parallel with nvcc (one -gencode, no cmake):
 
 * ``bt_step_f32.cu`` — FP32 step kernels (default -fmad=true)
 * ``bt_step_tma64.cu`` — the FP32 fast path for 64-wide tiles (narrow grids)
+* ``bt_step_tma_pal.cu`` — the FP32 fast path with per-voxel rates (rate palette)
 * ``bt_step_f64.cu`` — FP64 step kernels, -fmad=false so that no
   multiply-add contraction changes the reference's rounding
 * ``bt_api.cu``      — host runtime behind include/bt.h
@@ -35,6 +36,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.pat
 UNITS = [
     ("bt_step_f32.cu", ARCH + ["--ptxas-options=-v"]),
     ("bt_step_tma64.cu", ARCH),
+    ("bt_step_tma_pal.cu", ARCH),
     ("bt_step_f64.cu", ARCH + ["-fmad=false"]),
     ("bt_api.cu", ARCH),
     ("bt_noalloc.cu", ARCH),

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/bt.h"
@@ -85,6 +86,12 @@ struct bt_handle {
     // per-voxel mode: [8][nz][ny][pitch] in the handle's precision: dTime/T1,
     // dTime/T2, then the face diffusivities -x +x -y +y -z +z
     void* fields_d = nullptr;
+    // FP32 fast path with per-voxel rates: the rate palette (256 pairs of
+    // dTime/T1, dTime/T2) and each voxel's index into it ([nz][ny][cpitch]);
+    // pal_ok when the uploaded rates fit it (see bt_upload_rates)
+    uint8_t* pal_idx = nullptr;
+    float* pal_tab = nullptr;
+    bool pal_ok = false;
     void* pred_base = nullptr;    // MacCormack predictor field [batch][component][z][y][pitch]
     // two-component sums: weights [2][nz][ny][pitch], block partials, M(t) x 6
     void* weights_d = nullptr;
@@ -216,6 +223,7 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit, int zlong = 1 <
         P.fstride = (long long)h->comp;
         P.fdtt = h->fields_d ? static_cast<const T*>(h->fields_d) : nullptr;
         P.fw = h->fields_d ? static_cast<const T*>(h->fields_d) + 2 * h->comp : nullptr;
+        P.pal = h->pal_ok ? h->pal_tab : nullptr;
         P.wait_polls = h->wait_polls;
         P.phase_axes = h->phase_axes;
     }
@@ -278,6 +286,12 @@ bool build_maps(bt_handle* h) {
             cuuint64_t str[2] = {(cuuint64_t)h->cpitch, (cuuint64_t)h->cpitch * ny};
             cuuint32_t box[3] = {(cuuint32_t)h->ttx, (cuuint32_t)bt::tile_rows(h->ttx), 1};
             if (!encode(&M.code, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, h->code, dims, str, box)) return false;
+        }
+        if (h->pal_idx) {
+            cuuint64_t dims[3] = {nx, ny, nz};
+            cuuint64_t str[2] = {(cuuint64_t)h->cpitch, (cuuint64_t)h->cpitch * ny};
+            cuuint32_t box[3] = {(cuuint32_t)h->ttx, (cuuint32_t)bt::tile_rows(h->ttx), 1};
+            if (!encode(&M.pal, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, h->pal_idx, dims, str, box)) return false;
         }
         if (c.velocity == 1) {
             if (!h->ucell) return false;
@@ -377,14 +391,14 @@ cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
     const bt_config& c = h->cfg;
     const int prec = (c.scheme != BT_SCHEME_KSPACE && c.vector_mult == 1) ? 1 : 0;
     const int vel = c.velocity == 1 ? 1 : 0;
-    const bool fast = c.precision == BT_F32 && c.scheme != BT_SCHEME_MACCORMACK && h->use_tma && !h->fields_d &&
-                      !step_has_pulse(h, abs_step);
+    const bool fast = c.precision == BT_F32 && c.scheme != BT_SCHEME_MACCORMACK && h->use_tma &&
+                      (!h->fields_d || h->pal_ok) && !step_has_pulse(h, abs_step);
     cudaError_t e;
     if (fast) {
         // a fast step after a fast step adds its predecessor's partials
         h->launches++;
-        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->tgrid, h->ttx,
-                                !h->fast_pending, h->stream);
+        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->fields_d != nullptr, h->tgrid,
+                                h->ttx, !h->fast_pending, h->stream);
         h->fast_pending = true;
         h->fast_side = side;
         // the two-component sums read Ctl::step
@@ -805,6 +819,8 @@ int bt_destroy(bt_handle* h) {
     if (h->partials_d) cudaFree(h->partials_d);
     if (h->mt_d) cudaFree(h->mt_d);
     if (h->fields_d) cudaFree(h->fields_d);
+    if (h->pal_idx) cudaFree(h->pal_idx);
+    if (h->pal_tab) cudaFree(h->pal_tab);
     if (h->pred_base) cudaFree(h->pred_base);
     if (h->weights_d) cudaFree(h->weights_d);
     if (h->part6_d) cudaFree(h->part6_d);
@@ -821,6 +837,7 @@ int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, cons
     const bt_config& c = h->cfg;
     if (c.velocity == 1 && (!vx || !vy || !vz)) return fail(h, BT_E_ARG, "velocity == 1 needs vx, vy and vz");
     h->mask_h.assign(mask, mask + h->nvox);
+    h->pal_ok = false;  // a rate palette checked against another geometry no longer holds
     uint8_t* mtmp = nullptr;
     CK(h, cudaMalloc(&mtmp, h->nvox));
     cudaError_t e = cudaMemcpy(mtmp, mask, h->nvox, cudaMemcpyHostToDevice);
@@ -1136,6 +1153,62 @@ int put_pitched(bt_handle* h, void* dst, const std::vector<double>& src, int cou
     return BT_OK;
 }
 
+// The FP32 fast path takes per-voxel rates through a palette when they fit
+// one: the pore voxels' diffusivity is the configuration's (so the code
+// table's face weights hold), the solid voxels' is negligible (at most 1e-20
+// m^2/s: its face weights vanish in FP32 either way), and the pore voxels'
+// FP32 (dTime/T1, dTime/T2) pairs take at most 256 values. Then each voxel
+// gets its pair's index (solid voxels index 0: their update is zero) and the
+// fast path reads the pair from the palette; otherwise the generic kernel
+// reads the per-voxel fields.
+int build_palette(bt_handle* h, const std::vector<double>& buf, const double* diff) {
+    const bt_config& c = h->cfg;
+    h->pal_ok = false;
+    if (c.precision != BT_F32 || !fast_path_config(c) || h->mask_h.size() != h->nvox) return BT_OK;
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    const size_t comp = h->comp;
+    std::vector<uint8_t> idx((size_t)nz * ny * h->cpitch, 0);
+    std::vector<float> tab(512, 0.f);
+    std::unordered_map<uint64_t, int> seen;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t q = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
+                if (!h->mask_h[q]) {
+                    if (!(diff[q] <= 1e-20)) return BT_OK;
+                    continue;
+                }
+                if (diff[q] != c.d_pore) return BT_OK;
+                const size_t v = ((size_t)k * ny + j) * h->pitch + i;
+                const float r1 = (float)buf[v], r2 = (float)buf[comp + v];
+                uint32_t b1, b2;
+                std::memcpy(&b1, &r1, 4);
+                std::memcpy(&b2, &r2, 4);
+                const uint64_t key = ((uint64_t)b1 << 32) | b2;
+                auto it = seen.find(key);
+                int id;
+                if (it == seen.end()) {
+                    id = (int)seen.size();
+                    if (id >= 256) return BT_OK;
+                    seen.emplace(key, id);
+                    tab[2 * id] = r1;
+                    tab[2 * id + 1] = r2;
+                } else {
+                    id = it->second;
+                }
+                idx[((size_t)k * ny + j) * h->cpitch + i] = (uint8_t)id;
+            }
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (!h->pal_idx) CK(h, cudaMalloc(&h->pal_idx, idx.size()));
+    if (!h->pal_tab) CK(h, cudaMalloc(&h->pal_tab, 512 * sizeof(float)));
+    CK(h, cudaMemcpy(h->pal_idx, idx.data(), idx.size(), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->pal_tab, tab.data(), 512 * sizeof(float), cudaMemcpyHostToDevice));
+    // the tensor maps gain the palette index
+    if (h->use_tma) h->use_tma = build_maps(h);
+    h->pal_ok = h->use_tma;
+    return BT_OK;
+}
+
 }  // namespace
 
 int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const double* diff) {
@@ -1144,6 +1217,7 @@ int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const doub
         CK(h, cudaStreamSynchronize(h->stream));
         if (h->fields_d) cudaFree(h->fields_d);
         h->fields_d = nullptr;
+        h->pal_ok = false;
         refresh_params(h);
         return BT_OK;
     }
@@ -1176,6 +1250,8 @@ int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const doub
         CK(h, cudaMalloc(&h->fields_d, 8 * comp * h->esz));
     }
     int rc = put_pitched(h, h->fields_d, buf, 8);
+    if (rc) return rc;
+    rc = build_palette(h, buf, diff);
     if (rc) return rc;
     refresh_params(h);
     return BT_OK;

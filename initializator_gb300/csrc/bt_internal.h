@@ -120,6 +120,9 @@ struct StepParams {
     const T* fdtt;
     const T* fw;
     long long fstride;
+    // FP32 fast path with per-voxel rates: (dTime/T1, dTime/T2) pairs of the
+    // rate palette (256 pairs); the per-voxel palette index is staged by TMA
+    const float* pal;
     const T* orig[3];           // MacCormack corrector: the step's input field M
     // FP32 fast path: polls before a plane-ring wait gives up (RING_WAIT_POLLS
     // unless a test shortens it to see the timeout path run)
@@ -131,6 +134,7 @@ struct TmaMaps {
     CUtensorMap state;   // 4D {x, y, z, component} over the input field
     CUtensorMap ucell;   // 4D {x, y, z, axis} over the upwind cell velocities
     CUtensorMap code;
+    CUtensorMap pal;     // 3D {x, y, z} over the per-voxel rate palette index (uint8)
 };
 
 // launchers (bt_step_f32.cu / bt_step_f64.cu)
@@ -150,10 +154,14 @@ cudaError_t launch_phase_sums(const StepParams<T>& p, const T* w1, const T* w2, 
 // reads Ctl::step); each later one also reduces its predecessor's partials
 // into M(t); launch_tma_finish(last step's parameters) closes the run (the last
 // step's M(t), Ctl::step)
-cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
-                            int tw, bool first, cudaStream_t s);
+// pal: per-voxel rates through the rate palette (p.pal, m.pal)
+cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, bool pal,
+                            dim3 grid, int tw, bool first, cudaStream_t s);
 cudaError_t launch_step_tma64(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
                               bool first, cudaStream_t s);
+// the fast path's per-voxel-rate instances (bt_step_tma_pal.cu), both tile widths
+cudaError_t launch_step_tma_palette(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec,
+                                    dim3 grid, int tw, bool first, cudaStream_t s);
 cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_t s);
 // upwind cell velocities of the fast path from the face velocities, [axis][z][y][pitch]
 cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s);

@@ -72,7 +72,7 @@ constexpr int TAB_ROW = 12;         // floats per code-table row: 48 B, so 8 dis
 // voxels wide: 128 (one 32-lane warp per row, 8 rows) or 64 (16 lanes per
 // row, two rows per warp, 16 rows) for narrow grids, where a 128-wide tile
 // would leave many lanes idle. Every thread holds 4 voxels along x.
-template <int TW_>
+template <int TW_, bool PAL_ = false>
 struct Tile {
     static_assert(TW_ == 128 || TW_ == 64, "tile width");
     static constexpr int TW = TW_;
@@ -87,7 +87,10 @@ struct Tile {
     static constexpr int SZ_U = 3 * TH * TW * 4;  // upwind cell velocities, 3 axes
     static constexpr int OFF_CODE = OFF_U + SZ_U;
     static constexpr int SZ_CODE = TH * TW;
-    static constexpr int STAGE = (OFF_CODE + SZ_CODE + 127) / 128 * 128;
+    // per-voxel rate palette index (instances with per-voxel rates only)
+    static constexpr int OFF_PAL = (OFF_CODE + SZ_CODE + 127) / 128 * 128;
+    static constexpr int SZ_PAL = PAL_ ? TH * TW : 0;
+    static constexpr int STAGE = (OFF_PAL + SZ_PAL + 127) / 128 * 128;
     static constexpr int OFF_AUX = NSTAGE * STAGE;  // tables, barriers, reduction
     // aux layout (bytes from OFF_AUX)
     static constexpr int AUX_TAB = 0;                     // 128 rows: 6 face weights, dt/T1, dt/T2, their sum, 3 unused
@@ -97,7 +100,8 @@ struct Tile {
     static constexpr int AUX_RED = AUX_FLAGS + 128;       // 8 warps x 3 doubles
     static constexpr int AUX_EX = AUX_RED + 256;          // exp(-i k_x x), TW float2
     static constexpr int AUX_EZ = AUX_EX + 8 * TW;        // exp(-i k_z z), up to ZCHUNK_MAX float2
-    static constexpr int SMEM = OFF_AUX + AUX_EZ + 8 * ZCHUNK_MAX + 128;  // + 128 for the base alignment
+    static constexpr int AUX_PAL = AUX_EZ + 8 * ZCHUNK_MAX;  // rate palette: 256 (dt/T1, dt/T2) float2
+    static constexpr int SMEM = OFF_AUX + AUX_PAL + (PAL_ ? 8 * 256 : 0) + 128;  // + 128 for the base alignment
     static_assert(OFF_U % 128 == 0 && OFF_CODE % 128 == 0 && STAGE % 128 == 0, "TMA destinations 128-aligned");
     static_assert(TW + TH <= NT, "one phase-table entry per thread for x and y");
 };
@@ -180,7 +184,7 @@ static __global__ void cell_velocity_kernel(const StepParams<float> P, float* __
     }
 }
 
-template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK, int PH>
+template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK, int PH, bool PAL>
 __global__ void __launch_bounds__(tma::NT, 2)
     step_tma_kernel(const __grid_constant__ StepParams<float> P, const __grid_constant__ TmaMaps M, int first) {
     using namespace tma;
@@ -192,12 +196,13 @@ __global__ void __launch_bounds__(tma::NT, 2)
     constexpr bool phx = SCHEME == SCHEME_KSPACE && PH == PH_ALL;
     constexpr bool phz = SCHEME == SCHEME_KSPACE && PH != PH_NONE;
     constexpr bool ph_axis[3] = {phx, phx, phz};
-    using Tl = Tile<TWV>;
+    using Tl = Tile<TWV, PAL>;
     constexpr int TW = Tl::TW, TH = Tl::TH, LW = Tl::LW, RPW = Tl::RPW, SW = Tl::SW, SH = Tl::SH;
     constexpr int OFF_STATE = Tl::OFF_STATE, OFF_U = Tl::OFF_U, OFF_CODE = Tl::OFF_CODE, STAGE = Tl::STAGE;
     constexpr int SZ_STATE = Tl::SZ_STATE, SZ_U = Tl::SZ_U, SZ_CODE = Tl::SZ_CODE, OFF_AUX = Tl::OFF_AUX;
     constexpr int AUX_TAB = Tl::AUX_TAB, AUX_EY = Tl::AUX_EY, AUX_BARS = Tl::AUX_BARS, AUX_FLAGS = Tl::AUX_FLAGS;
-    constexpr int AUX_RED = Tl::AUX_RED, AUX_EX = Tl::AUX_EX, AUX_EZ = Tl::AUX_EZ;
+    constexpr int AUX_RED = Tl::AUX_RED, AUX_EX = Tl::AUX_EX, AUX_EZ = Tl::AUX_EZ, AUX_PAL = Tl::AUX_PAL;
+    constexpr int OFF_PAL = Tl::OFF_PAL, SZ_PAL = Tl::SZ_PAL;
     // TMA destinations must sit on 128-byte boundaries: align the dynamic
     // shared-memory base explicitly (the launch reserves 128 spare bytes)
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -210,6 +215,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
     double* red = reinterpret_cast<double*>(smem + OFF_AUX + AUX_RED);
     float2* s_ex = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_EX);
     float2* s_ez = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_EZ);
+    float2* s_pal = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_PAL);
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, w = tid >> 5;
@@ -238,7 +244,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
     const int xb = x0 + QX * xl;  // first of this thread's 4 voxels
     const int y = y0 + row;
 
-    uint32_t txbytes = SZ_STATE + SZ_CODE;
+    uint32_t txbytes = SZ_STATE + SZ_CODE + SZ_PAL;
     if constexpr (VEL) txbytes += SZ_U;
     auto issue = [&](int slot, int plane) {
         uint64_t* bar = &bars[slot];
@@ -247,6 +253,7 @@ __global__ void __launch_bounds__(tma::NT, 2)
         tma_load_5d(base + OFF_STATE, &M.state, bar, x0 - 4, y0 - 1, plane, 0, (int)b);
         if constexpr (VEL) tma_load_4d(base + OFF_U, &M.ucell, bar, x0, y0, plane, 0);
         tma_load_3d(base + OFF_CODE, &M.code, bar, x0, y0, plane);
+        if constexpr (PAL) tma_load_3d(base + OFF_PAL, &M.pal, bar, x0, y0, plane);
     };
     // ghost-layer kinds of this step (BCK instances; the first step of a run
     // from step 0 reads copies), set once the step index is known
@@ -294,6 +301,9 @@ __global__ void __launch_bounds__(tma::NT, 2)
         const float4 a = s_tab[3 * tid], c = s_tab[3 * tid + 1];
         s_tab[3 * tid + 2] = make_float4(((a.x + a.y) + (a.z + a.w)) + (c.x + c.y), 0.f, 0.f, 0.f);
     }
+    // the rate palette (per-voxel rates): one pair per thread
+    if constexpr (PAL) s_pal[tid] = make_float2(P.pal[2 * tid], P.pal[2 * tid + 1]);
+    static_assert(!PAL || NT == 256, "one palette entry per thread");
     // everything below reads what the previous step wrote (the field, the
     // step counter): wait until that grid has completed and its writes are
     // visible (returns at once when this launch has no programmatic
@@ -582,6 +592,8 @@ __global__ void __launch_bounds__(tma::NT, 2)
             }
         }
         const uint32_t code4 = *reinterpret_cast<const uint32_t*>(base + OFF_CODE + row * TW + QX * xl);
+        uint32_t pal4 = 0;
+        if constexpr (PAL) pal4 = *reinterpret_cast<const uint32_t*>(base + OFF_PAL + row * TW + QX * xl);
         float ux[QX] = {0.f, 0.f, 0.f, 0.f}, uy[QX] = {0.f, 0.f, 0.f, 0.f}, uz[QX] = {0.f, 0.f, 0.f, 0.f};
         if constexpr (VEL) {
             const float* ur = reinterpret_cast<const float*>(base + OFF_U) + row * TW + QX * xl;
@@ -601,7 +613,13 @@ __global__ void __launch_bounds__(tma::NT, 2)
             const uint32_t cd = (code4 >> (8 * i)) & 127u;
             const float4 ta = s_tab[3 * cd], tb = s_tab[3 * cd + 1];
             float wxm = ta.x, wxp = ta.y, wym = ta.z, wyp = ta.w, wzm = tb.x, wzp = tb.y;
-            const float dtt1 = tb.z, dtt2 = tb.w;
+            float dtt1 = tb.z, dtt2 = tb.w;
+            if constexpr (PAL) {
+                // per-voxel rates: the voxel's palette entry
+                const float2 r = s_pal[(pal4 >> (8 * i)) & 255u];
+                dtt1 = r.x;
+                dtt2 = r.y;
+            }
             if constexpr (VEL) {
                 // upwind: +face -min(u,0), -face +max(u,0), u the gated cell
                 // average (zero where the face it draws from is closed)
@@ -791,19 +809,42 @@ static inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, int smem, cud
     return cfg;
 }
 
-template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK = false, int PH = PH_ALL>
+template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK = false, int PH = PH_ALL, bool PAL = false>
 static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, bool first, cudaStream_t s) {
-    constexpr int smem = tma::Tile<TWV>::SMEM;
+    constexpr int smem = tma::Tile<TWV, PAL>::SMEM;
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH>,
+        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH, PAL>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         configured = true;
     }
     cudaLaunchAttribute attr[1];
     const cudaLaunchConfig_t cfg = pdl_config(grid, dim3(tma::NT), smem, s, attr);
-    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH>, p, m, first ? 1 : 0);
+    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH, PAL>, p, m, first ? 1 : 0);
+}
+
+// per-voxel rates (the rate palette): the reference scheme, and KSPACE with
+// copy faces
+template <int TWV>
+static cudaError_t launch_step_tma_pal(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec,
+                                       dim3 grid, bool first, cudaStream_t s) {
+    if (scheme == SCHEME_REF) {
+        if (vel && prec) return launch_tma_t<SCHEME_REF, true, true, TWV, false, PH_ALL, true>(p, m, grid, first, s);
+        if (vel) return launch_tma_t<SCHEME_REF, true, false, TWV, false, PH_ALL, true>(p, m, grid, first, s);
+        if (prec) return launch_tma_t<SCHEME_REF, false, true, TWV, false, PH_ALL, true>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_REF, false, false, TWV, false, PH_ALL, true>(p, m, grid, first, s);
+    }
+    if (p.phase_axes == PH_Z) {
+        if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, false, PH_Z, true>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_Z, true>(p, m, grid, first, s);
+    }
+    if (p.phase_axes == PH_NONE) {
+        if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, false, PH_NONE, true>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_NONE, true>(p, m, grid, first, s);
+    }
+    if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, false, PH_ALL, true>(p, m, grid, first, s);
+    return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_ALL, true>(p, m, grid, first, s);
 }
 
 // the fast path's kernels of one tile width

@@ -98,14 +98,23 @@ class RateCase:
     def rates(self, corr=None):
         """(t1, t2, diff) per coarse voxel for bt_upload_rates: bulk + plain
         coarse surface rate (rho / dx_c per coarse solid face) + the correction
-        corr (in units of rho / dx_f; None = 0), the surface part kept >= 0."""
+        corr (in units of rho / dx_f; None = 0), the surface part kept >= 0
+        and rounded onto at most 255 levels."""
         kw = self.kw
-        surf = self.count_c * (self.dxf / kw["dx"])  # in units of rho / dx_f
+        r = self.dxf / kw["dx"]  # one coarse solid face, in units of rho / dx_f
+        surf = self.count_c * r
+        pore = self.mask > 0
         if corr is not None:
             surf = np.maximum(surf + corr, 0.0)
+            # on a grid of r / k (k as large as keeps <= 255 levels up to the
+            # sample's largest rate), so that the rates fit the FP32 fast
+            # path's rate palette (256 pairs); the plain rates (multiples of
+            # r) stay exactly as they are
+            hi = float(surf[pore].max()) if pore.any() else 0.0
+            k = max(1, int(254.0 * r / hi)) if hi > 0 else 1
+            surf = (np.round(surf * (k / r)) / k) * r
         r1 = 1.0 / kw["t1"] + self.unit1 * surf
         r2 = 1.0 / kw["t2"] + self.unit2 * surf
-        pore = self.mask > 0
         t1 = np.where(pore, 1.0 / r1, 1e50)
         t2 = np.where(pore, 1.0 / r2, 1e50)
         diff = np.where(pore, kw["d_pore"], 1e-50)
