@@ -179,8 +179,13 @@ int bt_run_async(bt_handle* h, long long nsteps);
  * then uses dTime*(1/T1), dTime*(1/T2) and the harmonic-mean face diffusivities
  * 2*Da*Db/(Da+Db+1e-50) of ExplicitSimple (cpp:3174-3185), formed here in FP64 in
  * that order (domain faces pair a voxel with itself, as the ghost copy does).
- * All three NULL returns to the coefficients formed from bt_config. Such steps
- * run on the generic kernel (the FP32 TMA fast path is skipped). */
+ * All three NULL returns to the coefficients formed from bt_config; a new
+ * bt_upload_geometry drops uploaded rates too (upload them after it). FP32
+ * handles whose pore voxels all have the configuration's d_pore (solid voxels
+ * at most 1e-20 m^2/s) and whose pore voxels' FP32 rate pairs take at most 256
+ * values keep them as a rate palette (an 8-bit index per voxel, the code
+ * table's face weights) and stay on the TMA fast path; other rates run on
+ * the generic kernel, which reads the eight per-voxel fields. */
 int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const double* diff);
 
 /* Two-component M(t) (OutputX/Y/Z with NCOMP 2, cpp:3324-3350, written by

@@ -12,9 +12,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
-#include <unordered_map>
 #include <vector>
 
 #include "../../include/bt.h"
@@ -53,6 +54,7 @@ struct bt_handle {
     void* vel[3] = {};
     float* ucell = nullptr;       // fast path: gated cell velocities [axis][z][y][pitch]
     void* staging = nullptr;      // pinned host buffer: two halves of one component each (FP32 handles)
+    size_t staging_bytes = 0;
     cudaEvent_t stage_ev[2] = {}; // the last copy through each half
     bt::StepInfo* steps_d = nullptr;
     long long nsched = 0;
@@ -224,6 +226,7 @@ void fill_params(bt_handle* h, bt::StepParams<T>* p, int zsplit, int zlong = 1 <
         P.fdtt = h->fields_d ? static_cast<const T*>(h->fields_d) : nullptr;
         P.fw = h->fields_d ? static_cast<const T*>(h->fields_d) + 2 * h->comp : nullptr;
         P.pal = h->pal_ok ? h->pal_tab : nullptr;
+        P.pal_idx = h->pal_ok ? h->pal_idx : nullptr;
         P.wait_polls = h->wait_polls;
         P.phase_axes = h->phase_axes;
     }
@@ -391,14 +394,14 @@ cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
     const bt_config& c = h->cfg;
     const int prec = (c.scheme != BT_SCHEME_KSPACE && c.vector_mult == 1) ? 1 : 0;
     const int vel = c.velocity == 1 ? 1 : 0;
-    const bool fast = c.precision == BT_F32 && c.scheme != BT_SCHEME_MACCORMACK && h->use_tma &&
-                      (!h->fields_d || h->pal_ok) && !step_has_pulse(h, abs_step);
+    const bool fast = c.precision == BT_F32 && c.scheme != BT_SCHEME_MACCORMACK && h->use_tma && !h->fields_d &&
+                      !step_has_pulse(h, abs_step);
     cudaError_t e;
     if (fast) {
         // a fast step after a fast step adds its predecessor's partials
         h->launches++;
-        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->fields_d != nullptr, h->tgrid,
-                                h->ttx, !h->fast_pending, h->stream);
+        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->pal_ok, h->tgrid, h->ttx,
+                                !h->fast_pending, h->stream);
         h->fast_pending = true;
         h->fast_side = side;
         // the two-component sums read Ctl::step
@@ -612,18 +615,14 @@ bool any_phase(const bt_handle* h) {
     return false;
 }
 
-// dense [nz][ny][nx] host component <-> pitched device component
-// dst[q] = src[q] (a precision conversion) for q < n, over the host's cores
-// when the field is large, so that the host side of a transfer keeps up with
-// the copy engine
-template <typename D, typename S>
-void convert(D* dst, const S* src, size_t n) {
+// fn(a, b) over the slices [a, b) of [0, n), on up to 32 of the host's
+// cores with at least `grain` items each (on the calling thread alone when n
+// is small)
+template <typename F>
+void parallel_slices(size_t n, size_t grain, F fn) {
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const unsigned nt = (unsigned)std::max<size_t>(1, std::min<size_t>(std::min(hw, 32u), n >> 20));
-    auto part = [dst, src, n, nt](unsigned t) {
-        const size_t a = n * t / nt, b = n * (t + 1) / nt;
-        for (size_t q = a; q < b; ++q) dst[q] = (D)src[q];
-    };
+    const unsigned nt = (unsigned)std::max<size_t>(1, std::min<size_t>(std::min(hw, 32u), n / std::max<size_t>(1, grain)));
+    auto part = [&fn, n, nt](unsigned t) { fn(n * t / nt, n * (t + 1) / nt); };
     if (nt == 1) {
         part(0);
         return;
@@ -643,6 +642,64 @@ void convert(D* dst, const S* src, size_t n) {
     part(0);
     for (unsigned t : left) part(t);
     for (auto& t : ts) t.join();
+}
+
+// Pinned staging buffers of destroyed handles, kept for the next handle on
+// the same device (pinning hundreds of MB costs tens of ms, as much as a
+// short solve); a handle takes the smallest kept buffer that is large
+// enough. At most PINNED_KEEP bytes are kept; the rest are freed.
+constexpr size_t PINNED_KEEP = (size_t)2 << 30;
+std::mutex g_pinned_mu;
+struct Pinned {
+    int device;
+    size_t bytes;
+    void* p;
+};
+std::vector<Pinned> g_pinned;
+
+cudaError_t pinned_get(int device, size_t bytes, void** out) {
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        int best = -1;
+        for (int i = 0; i < (int)g_pinned.size(); ++i)
+            if (g_pinned[i].device == device && g_pinned[i].bytes >= bytes &&
+                (best < 0 || g_pinned[i].bytes < g_pinned[best].bytes))
+                best = i;
+        if (best >= 0) {
+            *out = g_pinned[best].p;
+            g_pinned.erase(g_pinned.begin() + best);
+            return cudaSuccess;
+        }
+    }
+    return cudaMallocHost(out, bytes);
+}
+
+void pinned_put(int device, size_t bytes, void* p) {
+    std::vector<void*> drop;
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        g_pinned.push_back({device, bytes, p});
+        size_t total = 0;
+        for (const Pinned& b : g_pinned) total += b.bytes;
+        // free the oldest beyond the bound
+        while (total > PINNED_KEEP && !g_pinned.empty()) {
+            total -= g_pinned.front().bytes;
+            drop.push_back(g_pinned.front().p);
+            g_pinned.erase(g_pinned.begin());
+        }
+    }
+    for (void* q : drop) cudaFreeHost(q);
+}
+
+// dense [nz][ny][nx] host component <-> pitched device component
+// dst[q] = src[q] (a precision conversion) for q < n, over the host's cores
+// when the field is large, so that the host side of a transfer keeps up with
+// the copy engine
+template <typename D, typename S>
+void convert(D* dst, const S* src, size_t n) {
+    parallel_slices(n, (size_t)1 << 20, [dst, src](size_t a, size_t b) {
+        for (size_t q = a; q < b; ++q) dst[q] = (D)src[q];
+    });
 }
 
 // host FP64 component -> device field. FP32 handles convert into staging half
@@ -770,7 +827,11 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
         }
     }
     if (cfg->precision == BT_F32) {
-        if (cudaMallocHost(&h->staging, 2 * 4 * h->nvox) != cudaSuccess) return bail(BT_E_NOMEM);
+        h->staging_bytes = 2 * 4 * h->nvox;
+        if (pinned_get(h->device, h->staging_bytes, &h->staging) != cudaSuccess) {
+            h->staging = nullptr;
+            return bail(BT_E_NOMEM);
+        }
         for (auto& e : h->stage_ev)
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bail(BT_E_CUDA);
     }
@@ -813,7 +874,7 @@ int bt_destroy(bt_handle* h) {
     if (h->pulses_d) cudaFree(h->pulses_d);
     if (h->ctl_d) cudaFree(h->ctl_d);
     if (h->ctl_h) cudaFreeHost(h->ctl_h);
-    if (h->staging) cudaFreeHost(h->staging);
+    if (h->staging) pinned_put(h->device, h->staging_bytes, h->staging);
     for (auto& e : h->stage_ev)
         if (e) cudaEventDestroy(e);
     if (h->partials_d) cudaFree(h->partials_d);
@@ -837,7 +898,13 @@ int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, cons
     const bt_config& c = h->cfg;
     if (c.velocity == 1 && (!vx || !vy || !vz)) return fail(h, BT_E_ARG, "velocity == 1 needs vx, vy and vz");
     h->mask_h.assign(mask, mask + h->nvox);
-    h->pal_ok = false;  // a rate palette checked against another geometry no longer holds
+    // per-voxel rates belong to the geometry they were uploaded with
+    if (h->fields_d || h->pal_ok) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (h->fields_d) cudaFree(h->fields_d);
+        h->fields_d = nullptr;
+        h->pal_ok = false;
+    }
     uint8_t* mtmp = nullptr;
     CK(h, cudaMalloc(&mtmp, h->nvox));
     cudaError_t e = cudaMemcpy(mtmp, mask, h->nvox, cudaMemcpyHostToDevice);
@@ -860,7 +927,7 @@ int bt_upload_geometry(bt_handle* h, const uint8_t* mask, const double* vx, cons
                 CK(h, cudaMemcpy2D(h->vel[a], p3[a] * 8, src[a], w3[a] * 8, w3[a] * 8, rows3[a], cudaMemcpyHostToDevice));
             } else {
                 std::vector<float> f(n);
-                for (size_t q = 0; q < n; ++q) f[q] = (float)src[a][q];
+                convert(f.data(), src[a], n);
                 CK(h, cudaMemcpy2D(h->vel[a], p3[a] * 4, f.data(), w3[a] * 4, w3[a] * 4, rows3[a],
                                    cudaMemcpyHostToDevice));
             }
@@ -1146,58 +1213,139 @@ int put_pitched(bt_handle* h, void* dst, const std::vector<double>& src, int cou
         CK(h, cudaMemcpy(dst, src.data(), n * 8, cudaMemcpyHostToDevice));
     } else {
         std::vector<float> f(n);
-        for (size_t q = 0; q < n; ++q) f[q] = (float)src[q];
+        convert(f.data(), src.data(), n);
         CK(h, cudaMemcpy(dst, f.data(), n * 4, cudaMemcpyHostToDevice));
     }
     (void)c;
     return BT_OK;
 }
 
-// The FP32 fast path takes per-voxel rates through a palette when they fit
+// Open-addressing table of at most 512 rate pairs (1024 slots): each key's
+// insertion index. The palette build looks up every pore voxel's pair.
+struct PairTable {
+    uint64_t key[1024];
+    int16_t val[1024];  // insertion index, -1 = empty slot
+    int n = 0;
+    PairTable() { std::fill(val, val + 1024, (int16_t)-1); }
+    static unsigned slot(uint64_t k) {
+        k ^= k >> 33;
+        k *= 0xff51afd7ed558ccdULL;
+        k ^= k >> 33;
+        return (unsigned)k & 1023u;
+    }
+    // the key's index, inserted as the next one if new; -1 if new and the
+    // table already holds cap keys
+    int find_or_add(uint64_t k, int cap) {
+        for (unsigned s = slot(k);; s = (s + 1) & 1023u) {
+            if (val[s] < 0) {
+                if (n >= cap) return -1;
+                key[s] = k;
+                val[s] = (int16_t)n;
+                return n++;
+            }
+            if (key[s] == k) return val[s];
+        }
+    }
+    int find(uint64_t k) const {
+        for (unsigned s = slot(k);; s = (s + 1) & 1023u) {
+            if (val[s] < 0) return -1;
+            if (key[s] == k) return val[s];
+        }
+    }
+};
+
+// FP32 handles take per-voxel rates through a rate palette when they fit
 // one: the pore voxels' diffusivity is the configuration's (so the code
 // table's face weights hold), the solid voxels' is negligible (at most 1e-20
 // m^2/s: its face weights vanish in FP32 either way), and the pore voxels'
-// FP32 (dTime/T1, dTime/T2) pairs take at most 256 values. Then each voxel
-// gets its pair's index (solid voxels index 0: their update is zero) and the
-// fast path reads the pair from the palette; otherwise the generic kernel
-// reads the per-voxel fields.
-int build_palette(bt_handle* h, const std::vector<double>& buf, const double* diff) {
+// FP32 (dTime*(1/T1), dTime*(1/T2)) pairs take at most 256 values. Then each
+// voxel gets its pair's index (solid voxels index 0: their update is zero),
+// and the fast path and the generic kernel read the pair from the palette;
+// otherwise the generic kernel reads the eight per-voxel fields.
+int build_palette(bt_handle* h, const double* t1, const double* t2, const double* diff) {
     const bt_config& c = h->cfg;
     h->pal_ok = false;
-    if (c.precision != BT_F32 || !fast_path_config(c) || h->mask_h.size() != h->nvox) return BT_OK;
+    if (c.precision != BT_F32 || c.scheme == BT_SCHEME_MACCORMACK || h->mask_h.size() != h->nvox) return BT_OK;
     const int nx = c.nx, ny = c.ny, nz = c.nz;
-    const size_t comp = h->comp;
-    std::vector<uint8_t> idx((size_t)nz * ny * h->cpitch, 0);
+    const double dTime = c.dt;
+    // the FP32 pair of voxel q, formed as the per-voxel fields form it
+    auto key_at = [&](size_t q) {
+        const float r1 = (float)(dTime * (1.0 / t1[q])), r2 = (float)(dTime * (1.0 / t2[q]));
+        uint32_t b1, b2;
+        std::memcpy(&b1, &r1, 4);
+        std::memcpy(&b2, &r2, 4);
+        return ((uint64_t)b1 << 32) | b2;
+    };
+    // pass 1, planes in parallel: each slice's distinct pairs in first-seen
+    // order (at most 257 kept: one more means no palette) and the diffusivity
+    // checks
+    const size_t grain = std::max<size_t>(1, ((size_t)1 << 18) / ((size_t)nx * ny));
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nsl = std::max<size_t>(1, std::min<size_t>(std::min(hw, 32u), (size_t)nz / grain));
+    std::vector<std::vector<uint64_t>> found(nsl);
+    std::vector<char> bad(nsl, 0);
+    parallel_slices(nsl, 1, [&](size_t sa, size_t sb) {
+        std::unique_ptr<PairTable> seen(new PairTable);
+        for (size_t sl = sa; sl < sb; ++sl) {
+            std::vector<uint64_t>& mine = found[sl];
+            *seen = PairTable();
+            uint64_t last = ~0ull;
+            for (int k = (int)(nz * sl / nsl); k < (int)(nz * (sl + 1) / nsl) && !bad[sl]; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) {
+                        const size_t q = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
+                        if (!h->mask_h[q]) {
+                            if (!(diff[q] <= 1e-20)) bad[sl] = 1;
+                            continue;
+                        }
+                        if (diff[q] != c.d_pore) bad[sl] = 1;
+                        const uint64_t key = key_at(q);
+                        if (key == last) continue;
+                        last = key;
+                        const int before = seen->n;
+                        const int at = seen->find_or_add(key, 257);
+                        if (at < 0) {
+                            bad[sl] = 1;
+                            break;
+                        }
+                        if (at == before) mine.push_back(key);
+                    }
+        }
+    });
+    // the palette: the slices' pairs in slice order, then first-seen order
+    std::unique_ptr<PairTable> id(new PairTable);
     std::vector<float> tab(512, 0.f);
-    std::unordered_map<uint64_t, int> seen;
-    for (int k = 0; k < nz; ++k)
-        for (int j = 0; j < ny; ++j)
-            for (int i = 0; i < nx; ++i) {
-                const size_t q = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
-                if (!h->mask_h[q]) {
-                    if (!(diff[q] <= 1e-20)) return BT_OK;
-                    continue;
-                }
-                if (diff[q] != c.d_pore) return BT_OK;
-                const size_t v = ((size_t)k * ny + j) * h->pitch + i;
-                const float r1 = (float)buf[v], r2 = (float)buf[comp + v];
-                uint32_t b1, b2;
-                std::memcpy(&b1, &r1, 4);
-                std::memcpy(&b2, &r2, 4);
-                const uint64_t key = ((uint64_t)b1 << 32) | b2;
-                auto it = seen.find(key);
-                int id;
-                if (it == seen.end()) {
-                    id = (int)seen.size();
-                    if (id >= 256) return BT_OK;
-                    seen.emplace(key, id);
-                    tab[2 * id] = r1;
-                    tab[2 * id + 1] = r2;
-                } else {
-                    id = it->second;
-                }
-                idx[((size_t)k * ny + j) * h->cpitch + i] = (uint8_t)id;
+    for (size_t sl = 0; sl < nsl; ++sl) {
+        if (bad[sl]) return BT_OK;
+        for (uint64_t key : found[sl]) {
+            const int before = id->n;
+            const int n = id->find_or_add(key, 256);
+            if (n < 0) return BT_OK;
+            if (n == before) {
+                const uint32_t b1 = (uint32_t)(key >> 32), b2 = (uint32_t)key;
+                std::memcpy(&tab[2 * n], &b1, 4);
+                std::memcpy(&tab[2 * n + 1], &b2, 4);
             }
+        }
+    }
+    // pass 2, planes in parallel: each voxel's index (solid voxels 0)
+    std::vector<uint8_t> idx((size_t)nz * ny * h->cpitch, 0);
+    parallel_slices((size_t)nz, grain, [&](size_t ka, size_t kb) {
+        uint64_t last = ~0ull;
+        int last_id = 0;
+        for (int k = (int)ka; k < (int)kb; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const size_t q = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
+                    if (!h->mask_h[q]) continue;
+                    const uint64_t key = key_at(q);
+                    if (key != last) {
+                        last = key;
+                        last_id = id->find(key);
+                    }
+                    idx[((size_t)k * ny + j) * h->cpitch + i] = (uint8_t)last_id;
+                }
+    });
     CK(h, cudaStreamSynchronize(h->stream));
     if (!h->pal_idx) CK(h, cudaMalloc(&h->pal_idx, idx.size()));
     if (!h->pal_tab) CK(h, cudaMalloc(&h->pal_tab, 512 * sizeof(float)));
@@ -1205,7 +1353,7 @@ int build_palette(bt_handle* h, const std::vector<double>& buf, const double* di
     CK(h, cudaMemcpy(h->pal_tab, tab.data(), 512 * sizeof(float), cudaMemcpyHostToDevice));
     // the tensor maps gain the palette index
     if (h->use_tma) h->use_tma = build_maps(h);
-    h->pal_ok = h->use_tma;
+    h->pal_ok = true;
     return BT_OK;
 }
 
@@ -1222,13 +1370,26 @@ int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const doub
         return BT_OK;
     }
     if (!t1 || !t2 || !diff) return fail(h, BT_E_ARG, "t1, t2 and diff are uploaded together");
+    if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    // rates that fit the rate palette need no per-voxel fields
+    int rc = build_palette(h, t1, t2, diff);
+    if (rc) return rc;
+    if (h->pal_ok) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (h->fields_d) cudaFree(h->fields_d);
+        h->fields_d = nullptr;
+        refresh_params(h);
+        return BT_OK;
+    }
     const bt_config& c = h->cfg;
     const int nx = c.nx, ny = c.ny, nz = c.nz;
     const size_t comp = h->comp;
     std::vector<double> buf(8 * comp, 0.0);
     const double dTime = c.dt;
     const double reg = c.scheme == BT_SCHEME_MACCORMACK ? 1.0e-25 : SMALL;
-    for (int k = 0; k < nz; ++k)
+    // planes in parallel on the host's cores
+    parallel_slices((size_t)nz, std::max<size_t>(1, ((size_t)1 << 18) / ((size_t)nx * ny)), [&](size_t ka, size_t kb) {
+    for (int k = (int)ka; k < (int)kb; ++k)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
                 const size_t q = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
@@ -1245,13 +1406,12 @@ int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const doub
                                       k < nz - 1 ? diff[q + (size_t)nx * ny] : Dc};
                 for (int f = 0; f < 6; ++f) buf[(2 + f) * comp + v] = 2.0 * (nb[f] * Dc) / (nb[f] + Dc + reg);
             }
+    });
     if (!h->fields_d) {
         drop_graphs(h);
         CK(h, cudaMalloc(&h->fields_d, 8 * comp * h->esz));
     }
-    int rc = put_pitched(h, h->fields_d, buf, 8);
-    if (rc) return rc;
-    rc = build_palette(h, buf, diff);
+    rc = put_pitched(h, h->fields_d, buf, 8);
     if (rc) return rc;
     refresh_params(h);
     return BT_OK;

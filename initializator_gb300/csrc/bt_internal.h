@@ -120,9 +120,11 @@ struct StepParams {
     const T* fdtt;
     const T* fw;
     long long fstride;
-    // FP32 fast path with per-voxel rates: (dTime/T1, dTime/T2) pairs of the
-    // rate palette (256 pairs); the per-voxel palette index is staged by TMA
+    // FP32 per-voxel rates through the rate palette: (dTime/T1, dTime/T2)
+    // pairs (256) and each voxel's index ([nz][ny][cpitch] like code; the
+    // fast path stages it by TMA); the face weights stay the code table's
     const float* pal;
+    const uint8_t* pal_idx;
     const T* orig[3];           // MacCormack corrector: the step's input field M
     // FP32 fast path: polls before a plane-ring wait gives up (RING_WAIT_POLLS
     // unless a test shortens it to see the timeout path run)

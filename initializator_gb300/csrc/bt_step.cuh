@@ -473,8 +473,14 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
             if (cd & CODE_PORE) {
                 const int f = cd & 63;
                 const long long vox = oz + col;
-                const T dtt1 = P.fdtt ? P.fdtt[vox] : P.dtt1[f];
-                const T dtt2 = P.fdtt ? P.fdtt[P.fstride + vox] : P.dtt2[f];
+                T dtt1 = P.fdtt ? P.fdtt[vox] : P.dtt1[f];
+                T dtt2 = P.fdtt ? P.fdtt[P.fstride + vox] : P.dtt2[f];
+                if (P.pal) {
+                    // FP32 per-voxel rates through the rate palette
+                    const int id = P.pal_idx[(long long)z * cplane + ccol];
+                    dtt1 = (T)P.pal[2 * id];
+                    dtt2 = (T)P.pal[2 * id + 1];
+                }
                 const T px0 = cc[0], py0 = cc[1], pz0 = cc[2];
                 // neighbours: -x +x -y +y -z +z, per component
                 T nb[3][6];

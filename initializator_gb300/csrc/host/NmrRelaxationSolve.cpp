@@ -21,7 +21,6 @@ namespace {
 
 const double kG = 4.78941714e+7;  // the reference's gyromagnetic constant (cpp:807)
 const double kSmall = 1.0e-50;
-const double kPi = 3.1415926535897932384626433832795028841971;
 
 double rmin(double a, double b) { return a <= b ? a : b; }  // NmrRelaxationSolve::min (cpp:3289-3293)
 

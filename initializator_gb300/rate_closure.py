@@ -89,8 +89,14 @@ class RateCase:
         v = 0.5 * (vy[:, :-1, :] + vy[:, 1:, :]) * c
         w = 0.5 * (vz[:-1, :, :] + vz[1:, :, :]) * c
         pore = self.mask.astype(np.float64)
-        self.features = np.stack([self.phi, self.count_c / 6, self.count_f / 6, pore, u, v, w,
-                                  np.sqrt(u * u + v * v + w * w)], axis=-1).astype(np.float32)
+        feats = np.stack([self.phi, self.count_c / 6, self.count_f / 6, pore, u, v, w,
+                          np.sqrt(u * u + v * v + w * w)], axis=-1).astype(np.float32)
+        # in page-locked host memory, so that the network's input copy runs at
+        # the copy engine's speed
+        import torch
+        self.features = torch.from_numpy(feats)
+        if torch.cuda.is_available():
+            self.features = self.features.pin_memory()
         # the surface rate unit: rho / dx_f per solid face of a fine voxel
         self.unit1 = case.kw["rho1"] / self.dxf
         self.unit2 = case.kw["rho2"] / self.dxf
@@ -102,6 +108,8 @@ class RateCase:
         and rounded onto at most 255 levels."""
         kw = self.kw
         r = self.dxf / kw["dx"]  # one coarse solid face, in units of rho / dx_f
+        if corr is not None and not isinstance(corr, np.ndarray):
+            return self._rates_device(corr, r)
         surf = self.count_c * r
         pore = self.mask > 0
         if corr is not None:
@@ -119,6 +127,27 @@ class RateCase:
         t2 = np.where(pore, 1.0 / r2, 1e50)
         diff = np.where(pore, kw["d_pore"], 1e-50)
         return t1, t2, diff
+
+    def _rates_device(self, corr, r):
+        """rates() for a correction already on the GPU (a torch tensor): the
+        same FP64 operations there, three host arrays back."""
+        import torch
+        kw = self.kw
+        dev = corr.device
+        if getattr(self, "_dev", None) is None or self._dev[0] != dev:
+            self._dev = (dev, torch.as_tensor(self.count_c, device=dev), torch.as_tensor(self.mask > 0, device=dev))
+        _, count_c, pore = self._dev
+        surf = torch.clamp(count_c * r + corr.double(), min=0.0)
+        hi = float(torch.where(pore, surf, torch.zeros_like(surf)).max()) if bool(pore.any()) else 0.0
+        k = max(1, int(254.0 * r / hi)) if hi > 0 else 1
+        surf = (torch.round(surf * (k / r)) / k) * r
+        r1 = 1.0 / kw["t1"] + self.unit1 * surf
+        r2 = 1.0 / kw["t2"] + self.unit2 * surf
+        big = torch.full_like(surf, 1e50)
+        t1 = torch.where(pore, 1.0 / r1, big)
+        t2 = torch.where(pore, 1.0 / r2, big)
+        diff = torch.where(pore, torch.full_like(surf, kw["d_pore"]), torch.full_like(surf, 1e-50))
+        return t1.cpu().numpy(), t2.cpu().numpy(), diff.cpu().numpy()
 
     def initial(self):
         st = np.zeros((3,) + self.shape)
@@ -197,7 +226,8 @@ class RateClosure:
         (nb, Z, Y, X) torch tensor, zero outside the pore."""
         import torch
         lay = C.PaddedRows(len(rcs), *rcs[0].shape)
-        x = lay.pack(np.stack([r.features for r in rcs]), self.net.device)
+        feats = [r.features for r in rcs]
+        x = lay.pack(feats[0].unsqueeze(0) if len(feats) == 1 else torch.stack(feats), self.net.device)
         y = lay.unpack(self.net.forward(lay, x), fp32_rows=True)[..., 0]
         pore = torch.as_tensor(np.stack([r.mask for r in rcs]), device=y.device).float()
         return self.scale * y * pore, lay, x
@@ -302,7 +332,7 @@ def time_to_mt(rc: RateCase, clo: RateClosure):
     e1.record()
     torch.cuda.synchronize()
     t_net = e0.elapsed_time(e1) / 1e3
-    cs = rc.solver(corr[0].double().cpu().numpy())
+    cs = rc.solver(corr[0])
     mt, t_cs = _timed_run(cs, rc.n)
     cs.close()
     t_learned = time.perf_counter() - t0

@@ -94,3 +94,22 @@ def test_rates_beyond_the_palette_stay_generic(btlib, monkeypatch):
     st_f, mt_f, n_f = _run(shape, case2, scheme, False, monkeypatch)
     assert n_f == n_g
     assert np.array_equal(st_f, st_g)
+
+
+def test_geometry_upload_drops_rates(btlib, monkeypatch):
+    """A new geometry drops per-voxel rates (palette and per-voxel fields):
+    the run then equals one with the configuration's uniform rates."""
+    import initializator_gb300 as bt
+    shape = (16, 24, 40)
+    for nclass in (7, 300):
+        mask, vel, st0, kw, rates, wave, rf = _case(shape, seed=9, nclass=nclass, scheme=0)
+        mts = []
+        for with_rates in (False, True):
+            with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, scheme=0, **kw)) as s:
+                s.upload_geometry(mask, vel)
+                if with_rates:
+                    s.upload_rates(*rates)
+                    s.upload_geometry(mask, vel)
+                s.set_state(st0)
+                mts.append(s.run(40))
+        assert np.array_equal(mts[0], mts[1])
