@@ -1507,19 +1507,23 @@ int bt_autotune(bt_handle* h, int trial_steps, int* best_chunks) {
         return BT_OK;
     }
     // candidate chunkings (chunks per field): for 1 to 8 waves of 2 CTAs per
-    // SM, the chunk count that fills exactly that many waves (tile columns
-    // differing by one chunk), and the even splits just below and just above
-    // it; chunks of >= 4 planes
+    // SM, and for the first four wave counts at which every tile column has a
+    // chunk (a batch's members share the waves), the chunk count that fills
+    // exactly that many waves (tile columns differing by one chunk) and the
+    // even splits just below and just above it; chunks of >= 4 planes
     const bt_config& c = h->cfg;
     const long long tiles = tma_tiles(h);
-    const long long slots = 2LL * h->num_sms / h->nb;  // CTA slots per member
+    const long long slots_all = 2LL * h->num_sms;  // CTA slots of the GPU
     std::vector<long long> cand;
     auto add = [&](long long chunks) {
         if (chunks >= tiles && chunks <= tiles * std::max(1, c.nz / 4)) cand.push_back(chunks);
     };
-    for (int waves = 1; waves <= 8; ++waves) {
-        const long long below = waves * slots / tiles;
-        add(waves * slots);
+    const long long w_min = (tiles * h->nb + slots_all - 1) / slots_all;  // waves with one chunk per column
+    for (long long waves = 1; waves <= std::max<long long>(8, w_min + 3); ++waves) {
+        if (waves > 8 && waves < w_min) continue;
+        const long long fill = waves * slots_all / h->nb;  // chunks per member
+        const long long below = fill / tiles;
+        add(fill);
         add(below * tiles);
         add((below + 1) * tiles);
     }
