@@ -187,6 +187,15 @@ int bt_run_async(bt_handle* h, long long nsteps);
  * table's face weights) and stay on the TMA fast path; other rates run on
  * the generic kernel, which reads the eight per-voxel fields. */
 int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const double* diff);
+/* Per-voxel rates given as a palette (no reference counterpart; the same
+ * result as bt_upload_rates with each pore voxel's T1, T2 taken from its entry
+ * and diff = d_pore in the pore): n (1..256) entries t1[e], t2[e] (s, host)
+ * and `idx`, a dense [nz][ny][nx] uint8 array in device memory holding each
+ * pore voxel's entry (< n; solid voxels ignored). FP32 handles, not the
+ * MacCormack scheme (BT_E_ARG otherwise); after bt_upload_geometry, which drops
+ * it. idx is read on the handle's stream (bt_stream) after the work already
+ * queued there, and the copy is complete on return. */
+int bt_upload_rate_palette(bt_handle* h, const double* t1, const double* t2, int n, const void* idx);
 
 /* Two-component M(t) (OutputX/Y/Z with NCOMP 2, cpp:3324-3350, written by
  * solve_gpu as "Time; X1; Y1; Z1; X2; Y2; Z2", cu:1211-1217): c1, c2 are the

@@ -69,7 +69,8 @@ class Conv3dArgs(ctypes.Structure):
 EXPORTS = [
     "bt_create", "bt_destroy", "bt_last_error", "bt_upload_geometry", "bt_set_state", "bt_get_state",
     "bt_set_state_device", "bt_set_schedule", "bt_step_index", "bt_set_step", "bt_run", "bt_run_async",
-    "bt_run_many", "bt_read_mt", "bt_synchronize", "bt_upload_rates", "bt_set_phase_weights",
+    "bt_run_many", "bt_read_mt", "bt_synchronize", "bt_upload_rates", "bt_upload_rate_palette",
+    "bt_set_phase_weights",
     "bt_read_mt_phases", "bt_stream", "bt_measure", "bt_launch_count", "bt_sequence_schedule",
     "bt_version", "bt_autotune", "bt_set_tma_split", "bt_set_tma_chunks", "bt_step_noalloc",
     "bt_conv3d_margin", "bt_conv3d", "bt_conv3d_weight_grad", "bt_conv3d_wgrad_scratch", "bt_conv3d_pack_weights",
@@ -104,6 +105,7 @@ def lib():
         "bt_run_async": ([vp, ll], i),
         "bt_run_many": ([ctypes.POINTER(vp), i, ll], i),
         "bt_upload_rates": ([vp, dp, dp, dp], i),
+        "bt_upload_rate_palette": ([vp, dp, dp, i, vp], i),
         "bt_set_phase_weights": ([vp, dp, dp], i),
         "bt_read_mt_phases": ([vp, dp, ll], i),
         "bt_read_mt": ([vp, dp, ll], i),
@@ -244,6 +246,20 @@ class Solver:
             return
         arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(self.shape) for a in (t1, t2, diff)]
         self._check(self._l.bt_upload_rates(self._h, *(_dp(a) for a in arrs)), "upload_rates")
+
+    def upload_rate_palette(self, t1, t2, idx):
+        """Per-voxel rates as a palette: entries t1[e], t2[e] (s, at most 256)
+        and idx, a (nz, ny, nx) uint8 CUDA tensor of each pore voxel's entry;
+        the pore diffusivity is the configuration's (FP32 handles)."""
+        import torch
+        t1 = np.ascontiguousarray(t1, dtype=np.float64)
+        t2 = np.ascontiguousarray(t2, dtype=np.float64)
+        assert t1.shape == t2.shape and t1.ndim == 1
+        assert idx.dtype == torch.uint8 and idx.is_cuda and tuple(idx.shape) == self.shape and idx.is_contiguous()
+        hs = self.torch_stream()
+        hs.wait_stream(torch.cuda.current_stream())
+        self._check(self._l.bt_upload_rate_palette(self._h, _dp(t1), _dp(t2), int(t1.size),
+                                                   ctypes.c_void_p(idx.data_ptr())), "upload_rate_palette")
 
     def set_phase_weights(self, c1=None, c2=None):
         """Two-component sums over c1 / c2 phase fractions, dense (nz, ny, nx); None switches off."""

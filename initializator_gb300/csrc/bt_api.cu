@@ -1417,6 +1417,34 @@ int bt_upload_rates(bt_handle* h, const double* t1, const double* t2, const doub
     return BT_OK;
 }
 
+int bt_upload_rate_palette(bt_handle* h, const double* t1, const double* t2, int n, const void* idx) {
+    if (!h) return BT_E_ARG;
+    const bt_config& c = h->cfg;
+    if (!t1 || !t2 || !idx || n < 1 || n > 256) return fail(h, BT_E_ARG, "a palette of 1..256 entries and its index");
+    if (c.precision != BT_F32 || c.scheme == BT_SCHEME_MACCORMACK)
+        return fail(h, BT_E_ARG, "rate palettes are for FP32 handles outside the MacCormack scheme");
+    if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
+    // each entry's FP32 pair, formed as the per-voxel fields form it
+    std::vector<float> tab(512, 0.f);
+    for (int e = 0; e < n; ++e) {
+        tab[2 * e] = (float)(c.dt * (1.0 / t1[e]));
+        tab[2 * e + 1] = (float)(c.dt * (1.0 / t2[e]));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->fields_d) cudaFree(h->fields_d);
+    h->fields_d = nullptr;
+    if (!h->pal_idx) CK(h, cudaMalloc(&h->pal_idx, (size_t)c.nz * c.ny * h->cpitch));
+    if (!h->pal_tab) CK(h, cudaMalloc(&h->pal_tab, 512 * sizeof(float)));
+    CK(h, cudaMemcpy2DAsync(h->pal_idx, h->cpitch, idx, c.nx, c.nx, (size_t)c.ny * c.nz, cudaMemcpyDeviceToDevice,
+                            h->stream));
+    CK(h, cudaMemcpyAsync(h->pal_tab, tab.data(), 512 * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));  // tab is a host temporary
+    if (h->use_tma) h->use_tma = build_maps(h);
+    h->pal_ok = true;
+    refresh_params(h);
+    return BT_OK;
+}
+
 int bt_set_phase_weights(bt_handle* h, const double* c1, const double* c2) {
     if (!h) return BT_E_ARG;
     if (!c1 && !c2) {

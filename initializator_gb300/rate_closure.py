@@ -128,6 +128,28 @@ class RateCase:
         diff = np.where(pore, kw["d_pore"], 1e-50)
         return t1, t2, diff
 
+    def palette_device(self, corr):
+        """The corrected rates of rates() as a rate palette, formed on the GPU:
+        the level entries' (t1, t2) (host arrays) and each voxel's level
+        (uint8 CUDA tensor), the same per-voxel values as rates(corr)."""
+        import torch
+        kw = self.kw
+        r = self.dxf / kw["dx"]
+        dev = corr.device
+        if getattr(self, "_dev", None) is None or self._dev[0] != dev:
+            self._dev = (dev, torch.as_tensor(self.count_c, device=dev), torch.as_tensor(self.mask > 0, device=dev))
+        _, count_c, pore = self._dev
+        surf = torch.clamp(count_c * r + corr.double(), min=0.0)
+        hi = float(torch.where(pore, surf, torch.zeros_like(surf)).max()) if bool(pore.any()) else 0.0
+        k = max(1, int(254.0 * r / hi)) if hi > 0 else 1
+        lev = torch.round(surf * (k / r))
+        n = int(lev[pore].max()) + 1 if bool(pore.any()) else 1
+        idx = torch.where(pore, lev, torch.zeros_like(lev)).to(torch.uint8).contiguous()
+        s_e = (np.arange(n, dtype=np.float64) / k) * r
+        t1 = 1.0 / (1.0 / kw["t1"] + self.unit1 * s_e)
+        t2 = 1.0 / (1.0 / kw["t2"] + self.unit2 * s_e)
+        return t1, t2, idx
+
     def _rates_device(self, corr, r):
         """rates() for a correction already on the GPU (a torch tensor): the
         same FP64 operations there, three host arrays back."""
@@ -159,7 +181,10 @@ class RateCase:
         from . import BT_F32, BT_SCHEME_KSPACE, Solver, make_config
         s = Solver(make_config(self.shape, precision=BT_F32, scheme=BT_SCHEME_KSPACE, **self.kw))
         s.upload_geometry(self.mask, self.vel)
-        s.upload_rates(*self.rates(corr))
+        if corr is not None and not isinstance(corr, np.ndarray):
+            s.upload_rate_palette(*self.palette_device(corr))  # the same rates, formed on the GPU
+        else:
+            s.upload_rates(*self.rates(corr))
         s.set_schedule(self.pulses, grad_wave=self.wave)
         s.set_state(self.initial())
         return s

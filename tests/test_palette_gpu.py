@@ -113,3 +113,39 @@ def test_geometry_upload_drops_rates(btlib, monkeypatch):
                 s.set_state(st0)
                 mts.append(s.run(40))
         assert np.array_equal(mts[0], mts[1])
+
+
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_palette_upload_matches_per_voxel_rates(scheme, btlib, monkeypatch):
+    """bt_upload_rate_palette (entries + a device index) gives the same run,
+    bit for bit, as bt_upload_rates with each voxel's entry spelled out; FP64
+    handles refuse it."""
+    import torch
+
+    import initializator_gb300 as bt
+    shape = (20, 33, 40)
+    mask, vel, st0, kw, _, wave, rf = _case(shape, seed=23, nclass=5, scheme=scheme)
+    rng = np.random.default_rng(4)
+    cls = rng.integers(0, 9, shape)
+    e1 = 0.04 + 0.013 * np.arange(9)
+    e2 = 0.015 + 0.005 * np.arange(9)
+    t1 = np.where(mask > 0, e1[cls], 1e50)
+    t2 = np.where(mask > 0, e2[cls], 1e50)
+    diff = np.where(mask > 0, kw["d_pore"], 1e-25)
+    out = []
+    for use_palette in (False, True):
+        with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, scheme=scheme, **kw)) as s:
+            s.upload_geometry(mask, vel)
+            if use_palette:
+                s.upload_rate_palette(e1, e2, torch.as_tensor(cls.astype(np.uint8), device="cuda"))
+            else:
+                s.upload_rates(t1, t2, diff)
+            s.set_schedule(rf, grad_wave=wave)
+            s.set_state(st0)
+            mt = s.run(64)
+            out.append((s.get_state(), mt))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    with bt.Solver(bt.make_config(shape, precision=bt.BT_F64, scheme=scheme, **kw)) as s:
+        s.upload_geometry(mask, vel)
+        with pytest.raises(bt.BtError):
+            s.upload_rate_palette(e1, e2, torch.as_tensor(cls.astype(np.uint8), device="cuda"))

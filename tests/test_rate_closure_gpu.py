@@ -63,3 +63,19 @@ def test_closure_beats_plain_coarse_on_held_out_seeds(trained, kind, seed, btlib
     learned, _ = rc.rollout(corr[0].double().cpu().numpy())
     e_plain, e_learned = R.mt_error(plain, ref), R.mt_error(learned, ref)
     assert e_learned < 0.5 * e_plain, (e_learned, e_plain)
+
+
+def test_palette_upload_equals_per_voxel_rates(trained, btlib):
+    """The timed path hands the corrected rates over as a rate palette formed
+    on the GPU; the rollout path as per-voxel host arrays. Same M(t), bit for
+    bit."""
+    R, C, clo, _ = trained
+    case = C.Case.pgse((32, 32, 32), seed=77, kind="sphere", g_amp=0.0, n_coarse=24, device="cuda")
+    rc = R.RateCase(case, 24)
+    corr, _, _ = clo.predict([rc])
+    mts = []
+    for c in (corr[0].double().cpu().numpy(), corr[0]):
+        s = rc.solver(c)
+        mts.append(s.run(24))
+        s.close()
+    assert np.array_equal(mts[0], mts[1])
