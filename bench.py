@@ -624,8 +624,12 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": list(SHAPE), "steps_per_iter": per,
-                   "note": "reference CPU update via the oracle port (the reference sources are not on the GPU box)"},
+        "config": {"workload": WORKLOAD, "grid": list(SHAPE), "steps_per_iter": per, "seed": SEED,
+                   "scheme": "the reference's update (ExplicitSimple: Euler cross-product precession), FP64",
+                   "l2": "inputs larger than L2", "parallelism": "host threads",
+                   "note": "reference CPU update via the oracle port (the reference sources are not on the GPU box); "
+                           "the same workload (geometry, flow, gradient waveform) as the GPU arm, sampled one time "
+                           "step per bench step"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{per} time step per bench step of the 256^3 workload, FP64, all host threads"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
