@@ -718,10 +718,21 @@ def run_ours(args):
     s.set_state(host_state)
     s.run(S)
     barrier()
+    # each bench step: the H2D of its input field (bt_set_state from host
+    # memory), S time steps, the D2H of its S M(t) samples (bt_read_mt). The
+    # next step's input is handed over while the GPU runs the current step:
+    # bt_set_state converts it on the host cores at once and queues its copy
+    # behind the running steps in the handle's stream order, and bt_read_mt
+    # then waits for the steps (and that copy) before the next run is queued
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s.set_state(host_state)  # H2D of the step's input field
-        s.run(S)                 # S time steps, D2H of the S M(t) samples
+    s.set_state(host_state)
+    s.run_async(S)
+    for i in range(args.steps):
+        if i + 1 < args.steps:
+            s.set_state(host_state)  # the next step's input
+        s.read_mt(S)                 # this step's M(t)
+        if i + 1 < args.steps:
+            s.run_async(S)
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s)

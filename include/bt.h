@@ -143,7 +143,10 @@ int bt_upload_geometry(bt_handle* h, const uint8_t* mask,
  * cpp:2472-2517, and the D2H copies of solve_gpu, cu:1193-1201).
  * bt_set_state returns once the host arrays have been read (they may be
  * reused at once); the device copy completes in the handle's stream order,
- * so a following bt_run / bt_get_state sees it. */
+ * so a following bt_run / bt_get_state sees it. Called while steps queued by
+ * bt_run_async still run, it converts the next field on the host meanwhile
+ * and its copy follows those steps (FP32 fields up to 2^26 voxels: one
+ * staging slot per component, so it does not wait for them). */
 int bt_set_state(bt_handle* h, const double* mx, const double* my, const double* mz);
 int bt_get_state(bt_handle* h, double* mx, double* my, double* mz);
 /* The same through device pointers of the handle's precision (float or

@@ -55,7 +55,17 @@ struct bt_handle {
     float* ucell = nullptr;       // fast path: gated cell velocities [axis][z][y][pitch]
     void* staging = nullptr;      // pinned host buffer: two halves of one component each (FP32 handles)
     size_t staging_bytes = 0;
-    cudaEvent_t stage_ev[2] = {}; // the last copy through each half
+    // staging slots of one component each: three (one per component, so a
+    // field's upload never waits for its own copies, and one uploaded while
+    // steps run returns once it is converted) up to 2^26 voxels, two above
+    int nstage = 2;
+    cudaEvent_t stage_ev[3] = {}; // the last copy through each slot
+    // FP32 single fields with three staging slots: bt_set_state copies into
+    // an inbox on a stream of its own (so the copy runs beside steps still
+    // queued) and the handle's stream moves it into the field after them
+    void* inbox = nullptr;
+    cudaStream_t xfer = nullptr;
+    cudaEvent_t in_ready = nullptr, inbox_free = nullptr;
     bt::StepInfo* steps_d = nullptr;
     long long nsched = 0;
     std::vector<bt::StepInfo> steps_h;
@@ -702,21 +712,21 @@ void convert(D* dst, const S* src, size_t n) {
     });
 }
 
-// host FP64 component -> device field. FP32 handles convert into staging half
+// host FP64 component -> device field. FP32 handles convert into staging slot
 // `half` (once the previous copy out of it has finished) and copy from there,
-// so consecutive components alternate halves and each conversion overlaps the
-// previous component's copy
-int put_component(bt_handle* h, void* dst, const double* src, int half) {
+// so consecutive components take consecutive slots and each conversion
+// overlaps the previous component's copy
+int put_component(bt_handle* h, void* dst, const double* src, int half, cudaStream_t s) {
     const bt_config& c = h->cfg;
     const size_t rows = (size_t)c.ny * c.nz;
     if (h->esz == 8) {
-        CK(h, cudaMemcpy2DAsync(dst, h->pitch * 8, src, c.nx * 8, c.nx * 8, rows, cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaMemcpy2DAsync(dst, h->pitch * 8, src, c.nx * 8, c.nx * 8, rows, cudaMemcpyHostToDevice, s));
     } else {
         float* f = static_cast<float*>(h->staging) + (size_t)half * h->nvox;
         CK(h, cudaEventSynchronize(h->stage_ev[half]));
         convert(f, src, h->nvox);
-        CK(h, cudaMemcpy2DAsync(dst, h->pitch * 4, f, c.nx * 4, c.nx * 4, rows, cudaMemcpyHostToDevice, h->stream));
-        CK(h, cudaEventRecord(h->stage_ev[half], h->stream));
+        CK(h, cudaMemcpy2DAsync(dst, h->pitch * 4, f, c.nx * 4, c.nx * 4, rows, cudaMemcpyHostToDevice, s));
+        CK(h, cudaEventRecord(h->stage_ev[half], s));
     }
     return BT_OK;
 }
@@ -827,7 +837,8 @@ int bt_create(const bt_config* cfg, bt_handle** out) {
         }
     }
     if (cfg->precision == BT_F32) {
-        h->staging_bytes = 2 * 4 * h->nvox;
+        h->nstage = h->nvox <= ((size_t)1 << 26) ? 3 : 2;
+        h->staging_bytes = (size_t)h->nstage * 4 * h->nvox;
         if (pinned_get(h->device, h->staging_bytes, &h->staging) != cudaSuccess) {
             h->staging = nullptr;
             return bail(BT_E_NOMEM);
@@ -864,6 +875,7 @@ int bt_destroy(bt_handle* h) {
     if (!h) return BT_OK;
     drop_graphs(h);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->xfer) cudaStreamSynchronize(h->xfer);  // its copies read the staging buffer
     for (auto& p : h->state_base)
         if (p) cudaFree(p);
     for (auto& p : h->vel)
@@ -886,6 +898,10 @@ int bt_destroy(bt_handle* h) {
     if (h->weights_d) cudaFree(h->weights_d);
     if (h->part6_d) cudaFree(h->part6_d);
     if (h->mt6_d) cudaFree(h->mt6_d);
+    if (h->xfer) cudaStreamDestroy(h->xfer);
+    if (h->in_ready) cudaEventDestroy(h->in_ready);
+    if (h->inbox_free) cudaEventDestroy(h->inbox_free);
+    if (h->inbox) cudaFree(h->inbox);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return BT_OK;
@@ -947,14 +963,37 @@ int bt_set_state(bt_handle* h, const double* mx, const double* my, const double*
     if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
     const double* src[3] = {mx, my, mz};
-    for (int b = 0; b < h->nb; ++b)
+    if (h->esz == 4 && h->nb == 1 && h->nstage == 3) {
+        // through the inbox: the host-to-device copies run on the transfer
+        // stream beside any steps still queued, then one device copy moves
+        // the field in after them
+        if (!h->inbox) {
+            CK(h, cudaMalloc(&h->inbox, 3 * h->comp * 4));
+            CK(h, cudaMemset(h->inbox, 0, 3 * h->comp * 4));  // the pitch padding stays zero
+            CK(h, cudaStreamCreateWithFlags(&h->xfer, cudaStreamNonBlocking));
+            CK(h, cudaEventCreateWithFlags(&h->in_ready, cudaEventDisableTiming));
+            CK(h, cudaEventCreateWithFlags(&h->inbox_free, cudaEventDisableTiming));
+            CK(h, cudaEventRecord(h->inbox_free, h->stream));
+        }
+        CK(h, cudaStreamWaitEvent(h->xfer, h->inbox_free, 0));  // the previous move out of the inbox
         for (int a = 0; a < 3; ++a) {
-            void* dst = (char*)h->state[h->cur][a] + (size_t)b * 3 * h->comp * h->esz;
-            int rc = put_component(h, dst, src[a] + (size_t)b * h->nvox, (3 * b + a) & 1);
+            int rc = put_component(h, (char*)h->inbox + (size_t)a * h->comp * 4, src[a], a, h->xfer);
             if (rc) return rc;
         }
+        CK(h, cudaEventRecord(h->in_ready, h->xfer));
+        CK(h, cudaStreamWaitEvent(h->stream, h->in_ready, 0));
+        CK(h, cudaMemcpyAsync(h->state_base[h->cur], h->inbox, 3 * h->comp * 4, cudaMemcpyDeviceToDevice, h->stream));
+        CK(h, cudaEventRecord(h->inbox_free, h->stream));
+    } else {
+        for (int b = 0; b < h->nb; ++b)
+            for (int a = 0; a < 3; ++a) {
+                void* dst = (char*)h->state[h->cur][a] + (size_t)b * 3 * h->comp * h->esz;
+                int rc = put_component(h, dst, src[a] + (size_t)b * h->nvox, (3 * b + a) % h->nstage, h->stream);
+                if (rc) return rc;
+            }
+    }
     // FP32: the host arrays have been read (converted into the staging
-    // halves); the copies and the frame change complete in the handle's
+    // slots); the copies and the frame change complete in the handle's
     // stream order. FP64 copies read the caller's arrays directly, so they
     // finish before the call returns.
     int rc = frame_change(h, h->state[h->cur], +1);
