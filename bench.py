@@ -553,6 +553,7 @@ def run_compat(args, lr):
 
 
 LEARNED_WEIGHTS = os.path.join(ROOT, "initializator_gb300", "data", "rate_closure_g0.npz")
+LEARNED_CHECK_EVERY = 50  # coarse steps between the learned solve's fine checks (checked timing)
 LEARNED_CASES = [((64, 64, 64), 250, "sphere", 900, 0.0), ((64, 64, 64), 250, "grf", 901, 0.0),
                  ((256, 256, 256), 250, "sphere", 902, 0.0), ((64, 64, 64), 250, "sphere", 900, 0.2)]
 
@@ -581,18 +582,22 @@ def run_learned(args, lr):
         rc = R.RateCase(case, n_coarse)
         ref = case.reference_mt(n_coarse)
         plain, _ = rc.rollout(None)
-        R.time_to_mt(rc, clo)  # warm-up
-        t, fine, learned = R.time_to_mt(rc, clo)
+        R.time_to_mt(rc, clo, check_every=LEARNED_CHECK_EVERY)  # warm-up
+        t, fine, learned = R.time_to_mt(rc, clo, check_every=LEARNED_CHECK_EVERY)
+        checked = t.pop("_checked_mt")
         rows.append({"grid": list(shape), "fine_steps": 4 * n_coarse, "geometry": kind, "seed": seed, "G": g,
                      "err_fine_f32": R.mt_error(fine, ref), "err_plain_coarse": R.mt_error(plain, ref),
-                     "err_learned": R.mt_error(learned, ref), **t,
+                     "err_learned": R.mt_error(learned, ref), "err_learned_checked": R.mt_error(checked, ref), **t,
                      "speedup": t["s_fine"] / t["s_learned"],
+                     "speedup_checked": t["s_fine"] / t["s_learned_checked"],
                      "speedup_steps": t["s_fine_steps"] / t["s_learned_steps"]})
         del case, rc
         torch.cuda.empty_cache()
     return {"definition": "err = max_t |M_xy(t) - M_xy,FP64 fine(t)| / |M_xy(first)|; time to M(t) after the "
                           "geometry is known (handle, upload, steps; the learned form adds the network); "
-                          "*_steps: device time of the steps (and the network) alone",
+                          "*_steps: device time of the steps (and the network) alone; *_checked: the learned "
+                          "solve with a fine check (prolong, 4 fine steps, compare) every 50 coarse steps and "
+                          "the fine solver as fallback",
             "weights": os.path.relpath(LEARNED_WEIGHTS, ROOT), "cases": rows}
 
 

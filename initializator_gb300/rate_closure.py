@@ -332,13 +332,58 @@ def _timed_run(s, nsteps):
     return s.read_mt(nsteps), e0.elapsed_time(e1) / 1e3
 
 
-def time_to_mt(rc: RateCase, clo: RateClosure):
+def solve_checked(rc: RateCase, corr, check_every=50, check_tol=1e-3):
+    """The corrected coarse solve with a periodic fine-step check, and the
+    fine solver as its fallback: at every check_every-th coarse step the
+    coarse field is prolonged to the fine grid (keeping its lab-frame sums)
+    and advanced 4 fine steps on a fine FP32 handle beside the coarse step;
+    when the two changes of the lab-frame sums differ by more than check_tol x
+    |M|, the curve goes on from there on the fine solver. corr: the
+    correction (None = the plain coarse solve). Returns (M(t) after each
+    coarse step, fine units; the coarse step of the fallback or None)."""
+    cs = rc.solver(corr)
+    fine = None
+    mt = np.zeros((rc.n, 3))
+    fell = None
+    n = 0
+    try:
+        while n < rc.n:
+            if n > 0 and n % check_every == 0:
+                if fine is None:
+                    fine = rc.case.solver(state=False)
+                fine.set_step(4 * n)
+                C._write_views(fine, cg.prolong(cs.field_views(), rc.case.k_at(4 * n), (rc.dxf,) * 3, rc.case.mask))
+                before = fine.measure()
+                after_f = fine.run(4)[-1]
+                mt[n] = 8.0 * cs.run(1)[0]
+                d = np.abs((mt[n] - before) - (after_f - before)).max()
+                if d > check_tol * max(np.abs(before).max(), 1e-300):
+                    fell = n
+                    mt[n] = after_f
+                    if n + 1 < rc.n:
+                        mt[n + 1:] = fine.run(4 * (rc.n - n - 1))[3::4]
+                    break
+                n += 1
+                continue
+            m = min(rc.n, (n // check_every + 1) * check_every) - n
+            mt[n:n + m] = 8.0 * cs.run(m)
+            n += m
+    finally:
+        cs.close()
+        if fine is not None:
+            fine.close()
+    return mt, fell
+
+
+def time_to_mt(rc: RateCase, clo: RateClosure, check_every=0):
     """Time to the M(t) curve of the sample once its geometry is known: the
     fine FP32 solve (handle, upload, 4 n fine steps) and the learned coarse
-    solve (network, handle with per-voxel rates, n coarse steps). Returns
-    {s_fine, s_learned: wall seconds of everything; s_fine_steps,
-    s_learned_steps: device seconds of the steps (and the network)}, fine
-    M(t), learned M(t)."""
+    solve (network, handle with per-voxel rates, n coarse steps); with
+    check_every, also the learned solve with its periodic fine check
+    (solve_checked). Returns {s_fine, s_learned: wall seconds of everything;
+    s_fine_steps, s_learned_steps: device seconds of the steps (and the
+    network); s_learned_checked, checked_fell_back_at, and the checked M(t)
+    under _checked_mt}, fine M(t), learned M(t)."""
     import time
 
     import torch
@@ -361,8 +406,19 @@ def time_to_mt(rc: RateCase, clo: RateClosure):
     mt, t_cs = _timed_run(cs, rc.n)
     cs.close()
     t_learned = time.perf_counter() - t0
-    return ({"s_fine": t_fine, "s_learned": t_learned, "s_fine_steps": t_fs, "s_learned_steps": t_net + t_cs},
-            fine, 8.0 * mt)
+    out = {"s_fine": t_fine, "s_learned": t_learned, "s_fine_steps": t_fs, "s_learned_steps": t_net + t_cs}
+    if check_every:
+        # the same with the periodic fine check (network, coarse handle, the
+        # fine check handle and its 4-step checks)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.no_grad():
+            corr, _, _ = clo.predict([rc])
+        checked, fell = solve_checked(rc, corr[0], check_every=check_every)
+        out.update({"s_learned_checked": time.perf_counter() - t0, "check_every": check_every,
+                    "checked_fell_back_at": fell})
+        out["_checked_mt"] = checked
+    return out, fine, 8.0 * mt
 
 
 def evaluate(shape=(64, 64, 64), n_coarse=88, n_train=8, outer=5, inner=120, g_test=0.2, seed=5, g_train=0.0,

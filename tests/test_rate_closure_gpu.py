@@ -80,3 +80,28 @@ def test_palette_upload_equals_per_voxel_rates(trained, btlib):
         mts.append(s.run(24))
         s.close()
     assert np.array_equal(mts[0], mts[1])
+
+
+def test_fine_check_falls_back_on_a_broken_closure(trained, btlib):
+    """The periodic fine check (prolong the coarse field, 4 fine steps,
+    compare the change of the lab-frame sums): the trained closure passes
+    every check; a broken correction (5 rho/dx_f more surface relaxation in
+    every pore voxel) fails the first one, the curve goes on on the fine
+    solver, and its error against the FP64 fine M(t) is less than half of the
+    unchecked broken solve's."""
+    import torch
+    R, C, clo, _ = trained
+    case = C.Case.pgse(SHAPE, seed=903, kind="sphere", g_amp=0.0, n_coarse=N_COARSE, device="cuda")
+    rc = R.RateCase(case, N_COARSE)
+    ref = case.reference_mt(N_COARSE)
+    corr, _, _ = clo.predict([rc])
+    good, fell = R.solve_checked(rc, corr[0], check_every=11)
+    assert fell is None
+    plain, _ = rc.rollout(None)
+    assert R.mt_error(good, ref) < 0.5 * R.mt_error(plain, ref)
+    broken = 5.0 * torch.as_tensor(rc.mask > 0, device=corr.device, dtype=torch.float32)
+    bad, fell_bad = R.solve_checked(rc, broken, check_every=10 ** 9)
+    assert fell_bad is None
+    chk, fell = R.solve_checked(rc, broken, check_every=11)
+    assert fell == 11
+    assert R.mt_error(chk, ref) < 0.5 * R.mt_error(bad, ref), (R.mt_error(chk, ref), R.mt_error(bad, ref))
