@@ -64,6 +64,7 @@ struct bt_handle {
     // an inbox on a stream of its own (so the copy runs beside steps still
     // queued) and the handle's stream moves it into the field after them
     void* inbox = nullptr;
+    bool no_inbox = false;        // no room for it on the device
     cudaStream_t xfer = nullptr;
     cudaEvent_t in_ready = nullptr, inbox_free = nullptr;
     bt::StepInfo* steps_d = nullptr;
@@ -963,12 +964,20 @@ int bt_set_state(bt_handle* h, const double* mx, const double* my, const double*
     if (!h || !mx || !my || !mz) return fail(h, BT_E_ARG, "null field");
     if (!h->geometry) return fail(h, BT_E_STATE, "bt_upload_geometry first");
     const double* src[3] = {mx, my, mz};
-    if (h->esz == 4 && h->nb == 1 && h->nstage == 3) {
+    bool use_inbox = h->esz == 4 && h->nb == 1 && h->nstage == 3 && !h->no_inbox;
+    if (use_inbox && !h->inbox && cudaMalloc(&h->inbox, 3 * h->comp * 4) != cudaSuccess) {
+        // the inbox only overlaps copies with steps: without room for it the
+        // copies go straight into the field
+        cudaGetLastError();
+        h->inbox = nullptr;
+        h->no_inbox = true;
+        use_inbox = false;
+    }
+    if (use_inbox) {
         // through the inbox: the host-to-device copies run on the transfer
         // stream beside any steps still queued, then one device copy moves
         // the field in after them
-        if (!h->inbox) {
-            CK(h, cudaMalloc(&h->inbox, 3 * h->comp * 4));
+        if (!h->xfer) {
             CK(h, cudaMemset(h->inbox, 0, 3 * h->comp * 4));  // the pitch padding stays zero
             CK(h, cudaStreamCreateWithFlags(&h->xfer, cudaStreamNonBlocking));
             CK(h, cudaEventCreateWithFlags(&h->in_ready, cudaEventDisableTiming));
