@@ -376,6 +376,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
         if (xb + i < nx && xb + i >= P.box[0] && xb + i < P.box[1]) xmask |= 1u << i;
     const bool row_sum = y < ny && y >= P.box[2] && y < P.box[3];
     const bool row_ok = y < ny;
+    // a warp whose rows all lie beyond the grid (the last tile row of a grid
+    // whose height is not a multiple of the tile's) skips the arithmetic and
+    // only keeps the ring going: its voxels are stored nowhere and add nothing
+    const bool warp_rows = __any_sync(0xffffffffu, row_ok);
     // threads holding a voxel on a domain face in x (lane 0 of the first
     // tile, the thread holding x = nx - 1); rows on a face in y are warp-uniform
     const bool x_lo = xb == 0;
@@ -748,8 +752,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
                 }
             }
         }
-        if (d > 0) body(prv, nxt);
-        else body(nxt, prv);
+        if (warp_rows) {
+            if (d > 0) body(prv, nxt);
+            else body(nxt, prv);
+        }
         release(sc);
         if (tid == 0 && q + NSTAGE < nplanes) refill(q + NSTAGE, sc, pc);
         sc = sn;
