@@ -184,7 +184,8 @@ int bt_run_async(bt_handle* h, long long nsteps);
  * that order (domain faces pair a voxel with itself, as the ghost copy does).
  * All three NULL returns to the coefficients formed from bt_config; a new
  * bt_upload_geometry drops uploaded rates too (upload them after it). FP32
- * handles whose pore voxels all have the configuration's d_pore (solid voxels
+ * handles (not the MacCormack scheme) whose pore voxels all have the
+ * configuration's d_pore (solid voxels
  * at most 1e-20 m^2/s) and whose pore voxels' FP32 rate pairs take at most 256
  * values keep them as a rate palette (an 8-bit index per voxel, the code
  * table's face weights) and stay on the TMA fast path; other rates run on
@@ -230,7 +231,8 @@ int bt_measure(bt_handle* h, double* sums3);
 
 /* Pick the z-chunking of the FP32 fast path by timing trial_steps steps for
  * each candidate (no reference counterpart: the reference launches one
- * thread per voxel, cu:1475-1476): for one to eight waves of CTAs, the chunk
+ * thread per voxel, cu:1475-1476): for one to eight waves of CTAs (and for a
+ * batch the first wave counts that give every tile column a chunk), the chunk
  * count that fills exactly that many waves and the even splits around it.
  * The field and step index are restored. *best_chunks (may be NULL) receives
  * the chosen number of chunks per field (as for bt_set_tma_chunks). */
