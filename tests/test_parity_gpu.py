@@ -606,3 +606,38 @@ def test_maccormack_per_voxel_fields(case, btlib, oracle_lib):
         assert rel_err(mt6, res[2]) <= F64_TOL
     else:
         assert rel_err(mt, res[1]) <= F64_TOL
+
+
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_state_upload_beside_running_steps(scheme, btlib):
+    """bt_set_state called while queued steps still run (the upload goes
+    through the inbox on the transfer stream and is moved in after them)
+    gives the same M(t) and fields, bit for bit, as the serial order."""
+    import initializator_gb300 as bt
+    shape = (24, 30, 70)
+    mask, vel, st0, kw = _random_case(shape, seed=31)
+    wave = None
+    if scheme == bt.BT_SCHEME_KSPACE:
+        kw.update(main_field=(0, 0, 1), vector_mult=0, gamma=bt.GAMMA_PROTON)
+        # a gradient, so that the second upload's frame change (at step 40)
+        # is not the identity
+        wave = bt.kspace_waveform_pgse(80, kw["dt"], 0.05, 8 * kw["dt"], 40 * kw["dt"], axis=(0.2, 0.5, 1.0))
+    st1 = np.roll(st0, 3, axis=3) * mask
+    outs = []
+    for overlap in (False, True):
+        with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, scheme=scheme, **kw)) as s:
+            s.upload_geometry(mask, vel)
+            if wave is not None:
+                s.set_schedule([], grad_wave=wave)
+            s.set_state(st0)
+            if overlap:
+                s.run_async(40)
+                s.set_state(st1)      # converted now, copied after the 40 steps
+                mt_a = s.read_mt(40)
+            else:
+                mt_a = s.run(40)
+                s.set_state(st1)
+            mt_b = s.run(40)
+            outs.append((mt_a, mt_b, s.get_state()))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
