@@ -181,12 +181,19 @@ class RateCase:
         from . import BT_F32, BT_SCHEME_KSPACE, Solver, make_config
         s = Solver(make_config(self.shape, precision=BT_F32, scheme=BT_SCHEME_KSPACE, **self.kw))
         s.upload_geometry(self.mask, self.vel)
-        if corr is not None and not isinstance(corr, np.ndarray):
+        on_device = corr is not None and not isinstance(corr, np.ndarray)
+        if on_device:
             s.upload_rate_palette(*self.palette_device(corr))  # the same rates, formed on the GPU
         else:
             s.upload_rates(*self.rates(corr))
         s.set_schedule(self.pulses, grad_wave=self.wave)
-        s.set_state(self.initial())
+        if on_device:
+            # the same FP32 initial field, formed on the GPU
+            import torch
+            mx = torch.as_tensor(self.phi, dtype=torch.float32, device=corr.device).contiguous()
+            s.set_state_device([mx, torch.zeros_like(mx), torch.zeros_like(mx)])
+        else:
+            s.set_state(self.initial())
         return s
 
     def lab_field(self, solver, n_done):

@@ -149,3 +149,34 @@ def test_palette_upload_matches_per_voxel_rates(scheme, btlib, monkeypatch):
         s.upload_geometry(mask, vel)
         with pytest.raises(bt.BtError):
             s.upload_rate_palette(e1, e2, torch.as_tensor(cls.astype(np.uint8), device="cuda"))
+
+
+def test_new_entry_points_check_their_arguments(btlib):
+    """bt_upload_rate_palette refuses 0 or more than 256 entries and a call
+    before the geometry; bt_set_tma_chunks clamps any count to a valid
+    chunking (fields bit-identical, M(t) within 1e-6: only the grouping of
+    the FP32 sums changes)."""
+    import torch
+
+    import initializator_gb300 as bt
+    shape = (16, 20, 40)
+    mask, vel, st0, kw, _, wave, rf = _case(shape, seed=41, nclass=3, scheme=0)
+    idx = torch.zeros(shape, dtype=torch.uint8, device="cuda")
+    with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, **kw)) as s:
+        with pytest.raises(bt.BtError):
+            s.upload_rate_palette([0.1], [0.05], idx)  # before the geometry
+        s.upload_geometry(mask, vel)
+        with pytest.raises(bt.BtError):
+            s.upload_rate_palette(np.zeros(0), np.zeros(0), idx)
+        with pytest.raises(bt.BtError):
+            s.upload_rate_palette(np.full(257, 0.1), np.full(257, 0.05), idx)
+        s.set_state(st0)
+        ref = s.run(20)
+        ref_st = s.get_state()
+        for ch in (-5, 1, 10 ** 7):
+            s.set_chunks(ch)
+            s.set_state(st0)
+            s.set_step(0)
+            mt = s.run(20)
+            assert np.array_equal(s.get_state(), ref_st)
+            assert rel_err(mt, ref) <= 1e-6
