@@ -10,6 +10,8 @@ namespace bt {
 constexpr int TX = 32;
 constexpr int TY = 8;
 constexpr int NTHREADS = TX * TY;
+// fixed-angle pulses of one step whose cosine and sine the step kernels form
+// once per CTA (any further ones in the same step take the per-voxel form)
 constexpr int MAX_PULSES_PER_STEP = 8;
 // default bound (polls) of the FP32 fast path's plane-ring waits; a healthy
 // copy lands in microseconds

@@ -59,14 +59,19 @@ struct Acc<double> {
 __device__ __forceinline__ float upsw(float v) { return v != 0.f ? 1.f : 0.f; }
 __device__ __forceinline__ double upsw(double v) { return v / (v + 1.0e-50); }
 
-// OrtTransform (cpp:2536-2550) in FP64
-__device__ __forceinline__ void ort(double& x, double& y, double& z, double nx, double ny, double nz, double angle) {
-    double c = cos(angle), s = sin(angle);
+// OrtTransform (cpp:2536-2550) with the angle's cosine c and sine s given
+__device__ __forceinline__ void ort_cs(double& x, double& y, double& z, double nx, double ny, double nz, double c,
+                                      double s) {
     double v0x = x, v0y = y, v0z = z;
     double scal = nx * v0x + ny * v0y + nz * v0z;
     x = v0x * c + nx * (1.0 - c) * scal + s * (ny * v0z - nz * v0y);
     y = v0y * c + ny * (1.0 - c) * scal + s * (nz * v0x - nx * v0z);
     z = v0z * c + nz * (1.0 - c) * scal + s * (nx * v0y - ny * v0x);
+}
+
+// OrtTransform (cpp:2536-2550) in FP64
+__device__ __forceinline__ void ort(double& x, double& y, double& z, double nx, double ny, double nz, double angle) {
+    ort_cs(x, y, z, nx, ny, nz, cos(angle), sin(angle));
 }
 
 // AddImpulse (cpp:2552-2608) for one voxel; x, y, z are 0-based cell indices
@@ -99,6 +104,84 @@ __device__ __forceinline__ void apply_pulse(const DevPulse& pu, double& mx, doub
         angle = 0.0 - g * sqrt(a * a + b * b + c * c);
         ort(mx, my, mz, ax, ay, az, angle);
     }
+}
+
+// A step's pulses, prepared once per CTA. A fixed-angle pulse (flag 2: angle
+// param about the axis as given) turns every voxel the same way, so the
+// cosine and sine of its angle are formed here once (FP64, by the functions
+// the per-voxel form calls, so the FP64 result is unchanged) instead of at
+// every voxel. For FP32 fields whose step holds only fixed-angle pulses, rot
+// is the product of their matrices c I + (1 - c) n n^T + s [n]x, formed in
+// FP64 and applied in FP32.
+struct PulsePrep {
+    double cs[MAX_PULSES_PER_STEP][2];
+    float rot[9];
+    int fixed_only;
+};
+
+// every thread of the CTA calls it (npulse > 0); a __syncthreads() follows
+__device__ __forceinline__ void pulse_prep(PulsePrep& pp, const DevPulse* pulses, int npulse, int tid) {
+    if (tid < npulse && tid < MAX_PULSES_PER_STEP && pulses[tid].flag == 2) {
+        pp.cs[tid][0] = cos(pulses[tid].param);
+        pp.cs[tid][1] = sin(pulses[tid].param);
+    }
+    if (tid == 0) {
+        bool fixed = npulse <= MAX_PULSES_PER_STEP;
+        double r[9] = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+        for (int q = 0; fixed && q < npulse; ++q) {
+            const DevPulse& pu = pulses[q];
+            if (pu.flag != 2) {
+                fixed = false;
+                break;
+            }
+            const double c = cos(pu.param), s = sin(pu.param);
+            const double n[3] = {pu.axis[0], pu.axis[1], pu.axis[2]};
+            double m[9];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) m[3 * i + j] = (i == j ? c : 0.0) + (1.0 - c) * n[i] * n[j];
+            m[1] -= s * n[2];
+            m[2] += s * n[1];
+            m[3] += s * n[2];
+            m[5] -= s * n[0];
+            m[6] -= s * n[1];
+            m[7] += s * n[0];
+            // later pulses act after earlier ones: r = m r
+            double t[9];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    t[3 * i + j] = m[3 * i] * r[j] + m[3 * i + 1] * r[3 + j] + m[3 * i + 2] * r[6 + j];
+            for (int i = 0; i < 9; ++i) r[i] = t[i];
+        }
+        for (int i = 0; i < 9; ++i) pp.rot[i] = (float)r[i];
+        pp.fixed_only = fixed ? 1 : 0;
+    }
+}
+
+// the step's pulses on one voxel's lab-frame (mx, my, mz), x, y, z 0-based
+template <typename T>
+__device__ __forceinline__ void apply_pulses(const PulsePrep& pp, const DevPulse* pulses, int npulse, T& mx_, T& my_,
+                                             T& mz_, int x, int y, int z, double dx, double dy, double dz, double g,
+                                             int nx, int ny, int nz) {
+    if constexpr (sizeof(T) == 4) {
+        if (pp.fixed_only) {
+            const float a = mx_, b = my_, c = mz_;
+            mx_ = pp.rot[0] * a + pp.rot[1] * b + pp.rot[2] * c;
+            my_ = pp.rot[3] * a + pp.rot[4] * b + pp.rot[5] * c;
+            mz_ = pp.rot[6] * a + pp.rot[7] * b + pp.rot[8] * c;
+            return;
+        }
+    }
+    double mx = mx_, my = my_, mz = mz_;
+    for (int q = 0; q < npulse; ++q) {
+        const DevPulse& pu = pulses[q];
+        if (pu.flag == 2 && q < MAX_PULSES_PER_STEP)
+            ort_cs(mx, my, mz, pu.axis[0], pu.axis[1], pu.axis[2], pp.cs[q][0], pp.cs[q][1]);
+        else
+            apply_pulse(pu, mx, my, mz, x, y, z, dx, dy, dz, g, nx, ny, nz);
+    }
+    mx_ = (T)mx;
+    my_ = (T)my;
+    mz_ = (T)mz;
 }
 
 // exp(-i * k * (c + 0.5) * d) with the argument formed and reduced in FP64
@@ -351,6 +434,7 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
     __shared__ T eys[TY][2];
     __shared__ T ezs[SCHEME == SCHEME_KSPACE ? ZCHUNK_MAX : 1][2];
     __shared__ int last_flag;
+    __shared__ PulsePrep pprep;
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TX + tx;
@@ -400,6 +484,10 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
     }
     const int npulse = si->pulse_count;
     const DevPulse* pulses = P.pulses + si->pulse_first;
+    if (npulse) {  // CTA-uniform
+        pulse_prep(pprep, pulses, npulse, tid);
+        __syncthreads();
+    }
     // non-copy domain faces take their own ghosts from the second step on (the
     // first step of a run from step 0 reads the reference's initial copies)
     const int bcs[3] = {P.bc[0], P.bc[1], P.bc[2]};
@@ -586,12 +674,8 @@ __global__ void __launch_bounds__(NTHREADS) step_kernel(const __grid_constant__ 
                     ly = er * ay + ei * ax;
                 }
                 if (npulse) {
-                    double mx = lx, my = ly, mz = az;
-                    for (int q = 0; q < npulse; ++q)
-                        apply_pulse(pulses[q], mx, my, mz, x, y, z, P.dxd, P.dyd, P.dzd, P.gamma, nx, ny, nz);
-                    lx = (T)mx;
-                    ly = (T)my;
-                    az = (T)mz;
+                    apply_pulses<T>(pprep, pulses, npulse, lx, ly, az, x, y, z, P.dxd, P.dyd, P.dzd, P.gamma, nx,
+                                    ny, nz);
                     if constexpr (SCHEME == SCHEME_KSPACE) {
                         ax = er * lx + ei * ly;  // back to the frame: conj(e) * lab
                         ay = er * ly - ei * lx;

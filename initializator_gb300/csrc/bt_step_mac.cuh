@@ -27,6 +27,7 @@ __global__ void __launch_bounds__(NTHREADS) mac_kernel(const __grid_constant__ S
     __shared__ T sm[3][TY + 2][TX + 2];
     __shared__ double red[NTHREADS / 32][3];
     __shared__ int last_flag;
+    __shared__ PulsePrep pprep;
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nx = P.nx, ny = P.ny, nz = P.nz;
@@ -65,6 +66,10 @@ __global__ void __launch_bounds__(NTHREADS) mac_kernel(const __grid_constant__ S
     }
     const int npulse = STAGE == 1 ? si->pulse_count : 0;
     const DevPulse* pulses = P.pulses + si->pulse_first;
+    if (npulse) {  // CTA-uniform
+        pulse_prep(pprep, pulses, npulse, ty * TX + tx);
+        __syncthreads();
+    }
     // non-copy domain faces: the predictor reads the field's ghosts, which
     // hold the reference's initial copies in the first step of a run from
     // step 0 (ghost layers are set at the end of each step); the corrector
@@ -208,14 +213,9 @@ __global__ void __launch_bounds__(NTHREADS) mac_kernel(const __grid_constant__ S
                     else o[c] = (T)0.5 * (orig[c][oz + col] + pa + rel + vec + dif + vel);
                 }
                 if constexpr (STAGE == 1) {
-                    if (npulse) {
-                        double mx = o[0], my = o[1], mz = o[2];
-                        for (int q = 0; q < npulse; ++q)
-                            apply_pulse(pulses[q], mx, my, mz, x, y, z, P.dxd, P.dyd, P.dzd, P.gamma, nx, ny, nz);
-                        o[0] = (T)mx;
-                        o[1] = (T)my;
-                        o[2] = (T)mz;
-                    }
+                    if (npulse)
+                        apply_pulses<T>(pprep, pulses, npulse, o[0], o[1], o[2], x, y, z, P.dxd, P.dyd, P.dzd,
+                                        P.gamma, nx, ny, nz);
                     if (in_box && z >= P.box[4] && z < P.box[5]) {
                         accx.add(o[0]);
                         accy.add(o[1]);

@@ -146,6 +146,52 @@ def test_kspace_matches_oracle_physics(precision, btlib, oracle_lib):
         assert rel_err(mt, ref_mt) <= F32_MT_TOL
 
 
+@pytest.mark.parametrize("scheme", [0, 1, 2])
+def test_several_pulses_in_one_step(scheme, btlib, oracle_lib):
+    """Steps holding several pulses, applied in the order given: three
+    fixed-angle pulses (one about an axis that is not a unit vector), which
+    FP32 fields take as one product rotation, and a fixed-angle pulse beside a
+    gradient-dependent one, which both precisions take in FP64 (the fixed
+    angle's cosine and sine formed once per CTA; KSPACE takes fixed-angle
+    pulses only, so there the second one is fixed-angle too). FP64 fields and M(t) within
+    1e-12 of the oracle (KSPACE: 1e-10, its k-frame bound); FP32 fields and
+    M(t) within 1e-4."""
+    import initializator_gb300 as bt
+    import oracle
+    pl = [(6, 2, 0.5 * math.pi, (1.0, 0.0, 0.0)), (6, 2, 0.3, (0.0, 0.6, 0.8)), (6, 2, math.pi, (0.2, 0.3, 0.9)),
+          (19, 2, 0.7, (0.0, 1.0, 0.0)), (19, 1, 2e-3, (0.2, -0.4, 0.9)), (31, 2, math.pi, (1.0, 0.0, 0.0))]
+    n = 40
+    if scheme == 1:
+        pl[4] = (19, 2, 1.1, (0.3, 0.0, 0.95))
+        shape = (20, 18, 36)
+        mask, vel, st0, kw, wave, _, _ = _kspace_case(shape, seed=4)
+        st0 = np.random.default_rng(4).uniform(-1, 1, (3,) + shape) * mask
+        p = oracle.make_params(shape, main_field=(0, 0, 1), vector_mult=2, **kw)
+        ref, ref_mt = oracle.run(p, mask, st0, n, vel=vel, pulses=pl, grad_wave=wave)
+        sched = dict(grad_wave=wave)
+        tol64 = KS64_TOL
+    else:
+        shape = (17, 22, 30)
+        mask, vel, st0, kw = _random_case(shape, seed=8)
+        p = oracle.make_params(shape, **kw)
+        ref, ref_mt = oracle.run(p, mask, st0, n, vel=vel, pulses=pl, maccormack=scheme == 2)
+        sched = {}
+        tol64 = F64_TOL
+    for prec in (bt.BT_F64, bt.BT_F32):
+        with bt.Solver(bt.make_config(shape, precision=prec, scheme=scheme, **kw)) as s:
+            s.upload_geometry(mask, vel)
+            s.set_schedule(pl, **sched)
+            s.set_state(st0)
+            mt = s.run(n)
+            st = s.get_state()
+        if prec == bt.BT_F64:
+            assert rel_err(st, ref) <= tol64
+            assert rel_err(mt, ref_mt) <= tol64
+        else:
+            assert rel_err(mt, ref_mt) <= F32_MT_TOL
+            assert rel_err(st, ref) <= F32_MT_TOL
+
+
 def test_kspace_state_roundtrip_mid_gradient(btlib):
     """set_state / get_state convert between the lab frame and the k frame."""
     import initializator_gb300 as bt
