@@ -37,6 +37,7 @@ UNITS = [
     ("bt_step_f32.cu", ARCH + ["--ptxas-options=-v"]),
     ("bt_step_tma64.cu", ARCH),
     ("bt_step_tma_pal.cu", ARCH),
+    ("bt_step_tma_rf.cu", ARCH + ["--ptxas-options=-v"]),
     ("bt_step_f64.cu", ARCH + ["-fmad=false"]),
     ("bt_api.cu", ARCH),
     ("bt_noalloc.cu", ARCH),

@@ -405,14 +405,17 @@ cudaError_t launch_one(bt_handle* h, int side, long long abs_step) {
     const bt_config& c = h->cfg;
     const int prec = (c.scheme != BT_SCHEME_KSPACE && c.vector_mult == 1) ? 1 : 0;
     const int vel = c.velocity == 1 ? 1 : 0;
+    // a pulse step runs on the fast path when all its pulses are fixed-angle
+    // (one rotation; not with the rate palette)
+    const bool pulse = step_has_pulse(h, abs_step);
     const bool fast = c.precision == BT_F32 && c.scheme != BT_SCHEME_MACCORMACK && h->use_tma && !h->fields_d &&
-                      !step_has_pulse(h, abs_step);
+                      (!pulse || (!h->pal_ok && h->steps_h[abs_step * h->nb].rot_ok));
     cudaError_t e;
     if (fast) {
         // a fast step after a fast step adds its predecessor's partials
         h->launches++;
-        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->pal_ok, h->tgrid, h->ttx,
-                                !h->fast_pending, h->stream);
+        e = bt::launch_step_tma(h->pt[side], h->maps[side], c.scheme, vel, prec, h->pal_ok, pulse, h->tgrid,
+                                h->ttx, !h->fast_pending, h->stream);
         h->fast_pending = true;
         h->fast_side = side;
         // the two-component sums read Ctl::step
@@ -527,6 +530,17 @@ int build_schedule(bt_handle* h, const bt_pulse* pulses, int npulses, const doub
             si.pulse_first = qi;
             while (qi < npulses && pulses[order[qi]].step == s) qi++;
             si.pulse_count = s < nsched ? qi - si.pulse_first : 0;
+            if (si.pulse_count > 0) {
+                // all fixed-angle: the FP32 fast path applies their product
+                double r[9] = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+                bool fixed = true;
+                for (int q = si.pulse_first; fixed && q < si.pulse_first + si.pulse_count; ++q) {
+                    fixed = dp[q].flag == 2;
+                    if (fixed) bt::fixed_pulse_then(std::cos(dp[q].param), std::sin(dp[q].param), dp[q].axis, r);
+                }
+                si.rot_ok = fixed ? 1 : 0;
+                for (int i = 0; i < 9; ++i) si.rotf[i] = (float)r[i];
+            }
         }
     }
     if (h->steps_d) cudaFree(h->steps_d);

@@ -47,7 +47,31 @@ struct StepInfo {
     float wrapf[3][2];
     int pulse_first;
     int pulse_count;
+    // FP32 fast path: when every pulse of the step is fixed-angle (flag 2),
+    // rot_ok = 1 and rotf is their product rotation (lab frame, row-major),
+    // formed in FP64 and rounded
+    int rot_ok;
+    float rotf[9];
 };
+
+// A fixed-angle pulse (flag 2: angle with cosine c and sine s about the axis
+// n as given, OrtTransform's cpp:2536-2550 rotation) acting after the
+// rotation r: r <- (c I + (1 - c) n n^T + s [n]x) r
+__host__ __device__ inline void fixed_pulse_then(double c, double s, const double n[3], double r[9]) {
+    double m[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) m[3 * i + j] = (i == j ? c : 0.0) + (1.0 - c) * n[i] * n[j];
+    m[1] -= s * n[2];
+    m[2] += s * n[1];
+    m[3] += s * n[2];
+    m[5] -= s * n[0];
+    m[6] -= s * n[1];
+    m[7] += s * n[0];
+    double t[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) t[3 * i + j] = m[3 * i] * r[j] + m[3 * i + 1] * r[3 + j] + m[3 * i + 2] * r[6 + j];
+    for (int i = 0; i < 9; ++i) r[i] = t[i];
+}
 
 // One pulse, with the reference's normalised axis precomputed on the host.
 struct DevPulse {
@@ -158,14 +182,18 @@ cudaError_t launch_phase_sums(const StepParams<T>& p, const T* w1, const T* w2, 
 // reads Ctl::step); each later one also reduces its predecessor's partials
 // into M(t); launch_tma_finish(last step's parameters) closes the run (the last
 // step's M(t), Ctl::step)
-// pal: per-voxel rates through the rate palette (p.pal, m.pal)
+// pal: per-voxel rates through the rate palette (p.pal, m.pal); rf: a pulse
+// step whose pulses are all fixed-angle (StepInfo::rotf; no palette)
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, bool pal,
-                            dim3 grid, int tw, bool first, cudaStream_t s);
+                            bool rf, dim3 grid, int tw, bool first, cudaStream_t s);
 cudaError_t launch_step_tma64(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, dim3 grid,
                               bool first, cudaStream_t s);
 // the fast path's per-voxel-rate instances (bt_step_tma_pal.cu), both tile widths
 cudaError_t launch_step_tma_palette(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec,
                                     dim3 grid, int tw, bool first, cudaStream_t s);
+// the fast path's pulse-step instances (bt_step_tma_rf.cu), both tile widths
+cudaError_t launch_step_tma_pulse(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec,
+                                  dim3 grid, int tw, bool first, cudaStream_t s);
 cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_t s);
 // upwind cell velocities of the fast path from the face velocities, [axis][z][y][pitch]
 cudaError_t launch_cell_velocity(const StepParams<float>& p, float* u, long long comp, cudaStream_t s);

@@ -38,7 +38,7 @@ namespace {
 
 constexpr size_t OFF_CTL = 0;                                     // bt::Ctl
 constexpr size_t OFF_STEP = 256;                                  // one bt::StepInfo
-constexpr size_t OFF_PULSE = 512;                                 // one bt::DevPulse
+constexpr size_t OFF_PULSE = 768;                                 // one bt::DevPulse
 constexpr size_t OFF_PARTIALS = 1024;                             // 3 doubles per CTA
 constexpr size_t OFF_CODE = OFF_PARTIALS + 3 * sizeof(double) * BT_NOALLOC_MAX_BLOCKS;
 constexpr size_t SCRATCH_BYTES = OFF_CODE + BT_NOALLOC_MAX_VOXELS;

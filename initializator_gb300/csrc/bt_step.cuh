@@ -111,8 +111,8 @@ __device__ __forceinline__ void apply_pulse(const DevPulse& pu, double& mx, doub
 // cosine and sine of its angle are formed here once (FP64, by the functions
 // the per-voxel form calls, so the FP64 result is unchanged) instead of at
 // every voxel. For FP32 fields whose step holds only fixed-angle pulses, rot
-// is the product of their matrices c I + (1 - c) n n^T + s [n]x, formed in
-// FP64 and applied in FP32.
+// is the product of their matrices (fixed_pulse_then), formed in FP64 and
+// applied in FP32.
 struct PulsePrep {
     double cs[MAX_PULSES_PER_STEP][2];
     float rot[9];
@@ -134,23 +134,7 @@ __device__ __forceinline__ void pulse_prep(PulsePrep& pp, const DevPulse* pulses
                 fixed = false;
                 break;
             }
-            const double c = cos(pu.param), s = sin(pu.param);
-            const double n[3] = {pu.axis[0], pu.axis[1], pu.axis[2]};
-            double m[9];
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) m[3 * i + j] = (i == j ? c : 0.0) + (1.0 - c) * n[i] * n[j];
-            m[1] -= s * n[2];
-            m[2] += s * n[1];
-            m[3] += s * n[2];
-            m[5] -= s * n[0];
-            m[6] -= s * n[1];
-            m[7] += s * n[0];
-            // later pulses act after earlier ones: r = m r
-            double t[9];
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j)
-                    t[3 * i + j] = m[3 * i] * r[j] + m[3 * i + 1] * r[3 + j] + m[3 * i + 2] * r[6 + j];
-            for (int i = 0; i < 9; ++i) r[i] = t[i];
+            fixed_pulse_then(cos(pu.param), sin(pu.param), pu.axis, r);
         }
         for (int i = 0; i < 9; ++i) pp.rot[i] = (float)r[i];
         pp.fixed_only = fixed ? 1 : 0;

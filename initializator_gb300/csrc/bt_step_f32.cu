@@ -56,7 +56,8 @@ cudaError_t launch_tma_finish(const StepParams<float>& p, dim3 grid, cudaStream_
 }
 
 cudaError_t launch_step_tma(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec, bool pal,
-                            dim3 grid, int tw, bool first, cudaStream_t s) {
+                            bool rf, dim3 grid, int tw, bool first, cudaStream_t s) {
+    if (rf) return launch_step_tma_pulse(p, m, scheme, vel, prec, grid, tw, first, s);
     if (pal) return launch_step_tma_palette(p, m, scheme, vel, prec, grid, tw, first, s);
     if (tw == 64) return launch_step_tma64(p, m, scheme, vel, prec, grid, first, s);
     return launch_step_tma_w<128>(p, m, scheme, vel, prec, grid, first, s);

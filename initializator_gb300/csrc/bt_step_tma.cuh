@@ -184,7 +184,7 @@ static __global__ void cell_velocity_kernel(const StepParams<float> P, float* __
     }
 }
 
-template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK, int PH, bool PAL>
+template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK, int PH, bool PAL, bool RF>
 __global__ void __launch_bounds__(tma::NT, 2)
     step_tma_kernel(const __grid_constant__ StepParams<float> P, const __grid_constant__ TmaMaps M, int first) {
     using namespace tma;
@@ -216,6 +216,9 @@ __global__ void __launch_bounds__(tma::NT, 2)
     float2* s_ex = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_EX);
     float2* s_ez = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_EZ);
     float2* s_pal = reinterpret_cast<float2*>(smem + OFF_AUX + AUX_PAL);
+    // RF: the step's pulse rotation, three rows (in the flag block's spare bytes)
+    float4* s_rot = reinterpret_cast<float4*>(smem + OFF_AUX + AUX_FLAGS + 16);
+    static_assert(AUX_FLAGS + 16 + 3 * 16 <= AUX_RED, "rotation rows fit the flag block");
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, w = tid >> 5;
@@ -323,6 +326,10 @@ __global__ void __launch_bounds__(tma::NT, 2)
             ky = P.bc[1];
             kz = P.bc[2];
         }
+    }
+    // a pulse step: every pulse fixed-angle, their product rotation
+    if constexpr (RF) {
+        if (tid < 3) s_rot[tid] = make_float4(si->rotf[3 * tid], si->rotf[3 * tid + 1], si->rotf[3 * tid + 2], 0.f);
     }
     if (tid == 0)
         for (int q = 0; q < NSTAGE && q < nplanes; ++q) {
@@ -612,6 +619,19 @@ __global__ void __launch_bounds__(tma::NT, 2)
         if (z_trim && (z < P.box[4] || z >= P.box[5])) smask = 0u;
         float o[3][QX];
         float sx_r = 0.f, sx_i = 0.f, sz_ = 0.f;  // this plane's sums over the 4 voxels
+        // RF, KSPACE: exp(-i (k_y y + k_z z)) of this row and plane
+        float rer = 1.f, rei = 0.f;
+        if constexpr (RF && SCHEME == SCHEME_KSPACE) {
+            if constexpr (phx) {
+                const float2 ey = s_ey[row], ez = s_ez[z - z0];
+                rer = ey.x * ez.x - ey.y * ez.y;
+                rei = ey.x * ez.y + ey.y * ez.x;
+            } else if constexpr (phz) {
+                const float2 ez = s_ez[z - z0];
+                rer = ez.x;
+                rei = ez.y;
+            }
+        }
 #pragma unroll
         for (int i = 0; i < QX; ++i) {
             const uint32_t cd = (code4 >> (8 * i)) & 127u;
@@ -696,6 +716,32 @@ __global__ void __launch_bounds__(tma::NT, 2)
             o[0][i] = pore ? ax : 0.f;
             o[1][i] = pore ? ay : 0.f;
             o[2][i] = pore ? az : 0.f;
+            if constexpr (RF) {
+                // the step's pulses act on the lab-frame value m_lab = e m,
+                // e = exp(-i k.r) this voxel's frame factor (1 for the
+                // reference scheme), and the result goes back: m = conj(e) m_lab
+                float er = rer, ei = rei, lr = o[0][i], li = o[1][i];
+                if constexpr (SCHEME == SCHEME_KSPACE) {
+                    if constexpr (phx) {
+                        er = exr[i] * rer - exi[i] * rei;
+                        ei = exr[i] * rei + exi[i] * rer;
+                    }
+                    lr = er * o[0][i] - ei * o[1][i];
+                    li = er * o[1][i] + ei * o[0][i];
+                }
+                const float lz = o[2][i];
+                const float4 r0 = s_rot[0], r1 = s_rot[1], r2 = s_rot[2];
+                const float nr = r0.x * lr + r0.y * li + r0.z * lz;
+                const float ni = r1.x * lr + r1.y * li + r1.z * lz;
+                o[2][i] = r2.x * lr + r2.y * li + r2.z * lz;
+                if constexpr (SCHEME == SCHEME_KSPACE) {
+                    o[0][i] = er * nr + ei * ni;
+                    o[1][i] = er * ni - ei * nr;
+                } else {
+                    o[0][i] = nr;
+                    o[1][i] = ni;
+                }
+            }
             const bool take = (smask >> i) & 1u;
             const float mr = take ? o[0][i] : 0.f, mi = take ? o[1][i] : 0.f;
             if constexpr (phx) {
@@ -815,19 +861,20 @@ static inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, int smem, cud
     return cfg;
 }
 
-template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK = false, int PH = PH_ALL, bool PAL = false>
+template <int SCHEME, bool VEL, bool PREC, int TWV, bool BCK = false, int PH = PH_ALL, bool PAL = false,
+          bool RF = false>
 static cudaError_t launch_tma_t(const StepParams<float>& p, const TmaMaps& m, dim3 grid, bool first, cudaStream_t s) {
     constexpr int smem = tma::Tile<TWV, PAL>::SMEM;
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH, PAL>,
+        cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH, PAL, RF>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         configured = true;
     }
     cudaLaunchAttribute attr[1];
     const cudaLaunchConfig_t cfg = pdl_config(grid, dim3(tma::NT), smem, s, attr);
-    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH, PAL>, p, m, first ? 1 : 0);
+    return cudaLaunchKernelEx(&cfg, step_tma_kernel<SCHEME, VEL, PREC, TWV, BCK, PH, PAL, RF>, p, m, first ? 1 : 0);
 }
 
 // per-voxel rates (the rate palette): the reference scheme, and KSPACE with
@@ -851,6 +898,21 @@ static cudaError_t launch_step_tma_pal(const StepParams<float>& p, const TmaMaps
     }
     if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, false, PH_ALL, true>(p, m, grid, first, s);
     return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_ALL, true>(p, m, grid, first, s);
+}
+
+// pulse steps of the fast path (every pulse of the step fixed-angle): the
+// general instances (KSPACE: any phase axes, any faces)
+template <int TWV>
+static cudaError_t launch_step_tma_rfw(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec,
+                                       dim3 grid, bool first, cudaStream_t s) {
+    if (scheme == SCHEME_REF) {
+        if (vel && prec) return launch_tma_t<SCHEME_REF, true, true, TWV, false, PH_ALL, false, true>(p, m, grid, first, s);
+        if (vel) return launch_tma_t<SCHEME_REF, true, false, TWV, false, PH_ALL, false, true>(p, m, grid, first, s);
+        if (prec) return launch_tma_t<SCHEME_REF, false, true, TWV, false, PH_ALL, false, true>(p, m, grid, first, s);
+        return launch_tma_t<SCHEME_REF, false, false, TWV, false, PH_ALL, false, true>(p, m, grid, first, s);
+    }
+    if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, true, PH_ALL, false, true>(p, m, grid, first, s);
+    return launch_tma_t<SCHEME_KSPACE, false, false, TWV, true, PH_ALL, false, true>(p, m, grid, first, s);
 }
 
 // the fast path's kernels of one tile width

@@ -150,12 +150,13 @@ def test_kspace_matches_oracle_physics(precision, btlib, oracle_lib):
 def test_several_pulses_in_one_step(scheme, btlib, oracle_lib):
     """Steps holding several pulses, applied in the order given: three
     fixed-angle pulses (one about an axis that is not a unit vector), which
-    FP32 fields take as one product rotation, and a fixed-angle pulse beside a
-    gradient-dependent one, which both precisions take in FP64 (the fixed
-    angle's cosine and sine formed once per CTA; KSPACE takes fixed-angle
-    pulses only, so there the second one is fixed-angle too). FP64 fields and M(t) within
-    1e-12 of the oracle (KSPACE: 1e-10, its k-frame bound); FP32 fields and
-    M(t) within 1e-4."""
+    FP32 fields take as one product rotation on the fast path, and a
+    fixed-angle pulse beside a gradient-dependent one, which both precisions
+    take in FP64 on the generic kernels (the fixed angle's cosine and sine
+    formed once per CTA; KSPACE takes fixed-angle pulses only, so there the
+    second one is fixed-angle too). FP64 fields and M(t) within 1e-12 of the
+    oracle (KSPACE: 1e-10, its k-frame bound); FP32 fields and M(t) within
+    1e-4."""
     import initializator_gb300 as bt
     import oracle
     pl = [(6, 2, 0.5 * math.pi, (1.0, 0.0, 0.0)), (6, 2, 0.3, (0.0, 0.6, 0.8)), (6, 2, math.pi, (0.2, 0.3, 0.9)),
@@ -190,6 +191,52 @@ def test_several_pulses_in_one_step(scheme, btlib, oracle_lib):
         else:
             assert rel_err(mt, ref_mt) <= F32_MT_TOL
             assert rel_err(st, ref) <= F32_MT_TOL
+
+
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_pulse_steps_on_the_fast_path(scheme, btlib, monkeypatch):
+    """FP32 steps whose pulses are all fixed-angle run on the fast path (the
+    step's rotation applied before its sums, the run of fast steps going on:
+    with a pulse in every 32-step window, n steps take n launches and one
+    closing launch) and give the generic kernel's fields and M(t) within
+    1e-5: a multi-echo train (a 90 at step 0, then a 180 every 8 steps) with
+    flow; KSPACE with a gradient along z, REFERENCE with the cross product."""
+    import initializator_gb300 as bt
+    from initializator_gb300 import geometry
+    shape = (40, 24, 48)
+    mask = geometry.sphere_pack(shape, 3.0, 0.3, seed=21)
+    vel = geometry.curl_velocity(mask, 2.0, 1e-3, seed=22)
+    dt = geometry.stable_dt(1e-6, 2.3e-9)
+    n = 64
+    kw = dict(dx=1e-6, dt=dt, d_pore=2.3e-9, t1=2.5, t2=2.0, rho1=1e-5, rho2=1e-5, p_eq=1.0, velocity=1,
+              diffusion=1)
+    rf = [(0, 2, 0.5 * math.pi, (0.0, 1.0, 0.0))] + [(q, 2, math.pi, (1.0, 0.0, 0.0)) for q in range(4, n, 8)]
+    sched = {}
+    if scheme == bt.BT_SCHEME_KSPACE:
+        kw.update(gamma=bt.GAMMA_PROTON)
+        sched = dict(grad_wave=bt.kspace_waveform_pgse(n, dt, 0.1, 6 * dt, 30 * dt, axis=(0.0, 0.0, 1.0)))
+    else:
+        kw.update(main_field=(0.2, 0.3, 0.9), grad=(0.02, -0.03, 0.05), vector_mult=1)
+    st0 = np.zeros((3,) + shape)
+    st0[2] = mask
+    out = []
+    for no_tma in (True, False):
+        if no_tma:
+            monkeypatch.setenv("BT_NO_TMA", "1")
+        else:
+            monkeypatch.delenv("BT_NO_TMA", raising=False)
+        with bt.Solver(bt.make_config(shape, precision=bt.BT_F32, scheme=scheme, **kw)) as s:
+            s.upload_geometry(mask, vel)
+            s.set_schedule(rf, **sched)
+            s.set_state(st0)
+            l0 = s.launches
+            mt = s.run(n)
+            n_run = s.launches - l0  # (get_state adds a frame change in KSPACE)
+            out.append((s.get_state(), mt, n_run))
+    (st_g, mt_g, _), (st_f, mt_f, n_f) = out
+    assert n_f == n + 1, n_f
+    assert rel_err(st_f, st_g) <= 1e-5
+    assert rel_err(mt_f, mt_g) <= 1e-5
 
 
 def test_kspace_state_roundtrip_mid_gradient(btlib):
