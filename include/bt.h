@@ -108,7 +108,11 @@ typedef struct bt_config {
  * (AddImpulse flag/param/axis, cpp:2552-2608): flag 1 linear-gradient phase
  * param*g*(x*dx*ax + y*dy*ay + z*dz*az) about the normalised axis; flag 2 RF
  * rotation by param about axis; flags 3 and 4 as the reference. The
- * KSPACE scheme accepts flag 2 only (gradients come from the waveform). */
+ * KSPACE scheme accepts flag 2 only (gradients come from the waveform).
+ * Several pulses of one step apply in the order given. On FP32 handles a
+ * step whose pulses are all flag 2 stays on the TMA fast path (their product
+ * rotation, formed in FP64, applied in FP32); other pulse steps, and pulse
+ * steps of handles with a rate palette, run on the generic kernel. */
 typedef struct bt_pulse {
     long long step;
     int flag;
@@ -279,7 +283,8 @@ long long bt_launch_count(const bt_handle* h);
 #define BT_NOALLOC_MAX_BLOCKS 16384       /* CTAs of the step kernel's grid */
 
 /* One step of the REFERENCE-scheme update (the fused kernel bt_run uses for
- * FP64 and for pulse steps) that performs no device allocation. No
+ * FP64 and for the FP32 steps the fast path does not take) that performs no
+ * device allocation. No
  * counterpart in the reference: it exists for callers that may not call
  * cudaMalloc — code running under CUDA stream capture, hosts whose framework
  * has reserved the device's memory for its own pool, plugin hosts that forbid
