@@ -363,6 +363,48 @@ def run_c5(args, lr):
                          "peak_kind": peak_kind, "bytes_per_voxel_step": BYTES_PER_VOXEL_STEP}}
 
 
+CPMG_ECHO = 10               # steps between the multi-echo leg's refocusing pulses
+CPMG_G = 0.05                # T/m, its constant gradient along z
+
+
+def run_cpmg(s, stream, st0, nvox, value_plain):
+    """Multi-echo (CPMG) train on the C2 handle (same geometry, flow and
+    z-chunking): a 90-degree pulse about y at step 0, then a 180-degree pulse
+    about x every CPMG_ECHO steps, under a constant gradient along z; one
+    warm-up iteration of STEPS_PER_ITER steps, then 2 x STEPS_PER_ITER timed
+    steps (CUDA events). A step whose pulses are all fixed-angle stays on the
+    fast path, so the train should run near the pulse-free rate; reported
+    with its ratio to the C2 value. No 32-step window is pulse-free, so every
+    step is its own launch (no CUDA graph)."""
+    import torch
+    S = STEPS_PER_ITER
+    n = 3 * S
+    wave = np.zeros((n + 16, 3))
+    wave[:, 2] = CPMG_G
+    rf = [(0, 2, 0.5 * math.pi, (0.0, 1.0, 0.0))]
+    rf += [(q, 2, math.pi, (1.0, 0.0, 0.0)) for q in range(CPMG_ECHO // 2, n, CPMG_ECHO)]
+    s.set_step(0)
+    s.set_schedule(rf, grad_wave=wave)
+    s.set_state(st0)
+    s.run_async(S)
+    s.synchronize()
+    l0 = s.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    s.run_async(2 * S)
+    ev1.record(stream)
+    s.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = s.launches - l0
+    mt = s.read_mt(2 * S)
+    v = nvox * 2 * S / (ms / 1e3)
+    return {"workload": f"C2 handle, CPMG: 90y at step 0, 180x every {CPMG_ECHO} steps, G = {CPMG_G} T/m along z, "
+                        f"{2 * S} timed steps", "value": v, "unit": UNIT, "ms_per_time_step": ms / (2 * S),
+            "pulse_steps": sum(1 for q, *_ in rf if S <= q < 3 * S), "launches": launches,
+            "vs_pulse_free": v / value_plain, "finite": bool(np.all(np.isfinite(mt)))}
+
+
 def physics(total_steps):
     import initializator_gb300 as bt
     from initializator_gb300 import geometry
@@ -742,6 +784,7 @@ def run_ours(args):
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s)
     e2e = job_value(nvox * S * args.steps, w, e2e_s)
+    cpmg = None if args.no_cpmg else run_cpmg(s, stream, st0, nvox, value / w)  # this rank's pulse-free rate
     s.close()
     # the benched kernel's M(t) against an FP64 run of the same solver, over
     # the whole 5000-step C2 run (a separate waveform of that length)
@@ -776,6 +819,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "clocks": clk,
             "mt_rel_err_vs_f64": err_c2,
+            "cpmg": cpmg,
             "qsweep": qsweep,
             "ragged": ragged,
             "c5": c5,
@@ -798,6 +842,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-qsweep", action="store_true", help="skip the batched 32-gradient q-sweep (C3a) leg")
+    ap.add_argument("--no-cpmg", action="store_true",
+                    help="skip the multi-echo train (a 180-degree pulse every 10 steps) on the C2 handle")
     ap.add_argument("--no-ragged", action="store_true", help="skip the 48-sample ragged batch (C3b) leg")
     ap.add_argument("--no-c5", action="store_true", help="skip the 1024x1024x768 (C5, ~100 GB with its FP64 check) leg")
     ap.add_argument("--no-learned", action="store_true",
