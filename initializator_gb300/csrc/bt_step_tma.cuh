@@ -900,8 +900,10 @@ static cudaError_t launch_step_tma_pal(const StepParams<float>& p, const TmaMaps
     return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_ALL, true>(p, m, grid, first, s);
 }
 
-// pulse steps of the fast path (every pulse of the step fixed-angle): the
-// general instances (KSPACE: any phase axes, any faces)
+// pulse steps of the fast path (every pulse of the step fixed-angle): KSPACE
+// with copy faces takes the instance of its phase axes when they are z or
+// none (PGSE and multi-echo schedules), else the general one (any phase axes,
+// any faces)
 template <int TWV>
 static cudaError_t launch_step_tma_rfw(const StepParams<float>& p, const TmaMaps& m, int scheme, int vel, int prec,
                                        dim3 grid, bool first, cudaStream_t s) {
@@ -910,6 +912,16 @@ static cudaError_t launch_step_tma_rfw(const StepParams<float>& p, const TmaMaps
         if (vel) return launch_tma_t<SCHEME_REF, true, false, TWV, false, PH_ALL, false, true>(p, m, grid, first, s);
         if (prec) return launch_tma_t<SCHEME_REF, false, true, TWV, false, PH_ALL, false, true>(p, m, grid, first, s);
         return launch_tma_t<SCHEME_REF, false, false, TWV, false, PH_ALL, false, true>(p, m, grid, first, s);
+    }
+    if (p.bc[0] == BC_COPY && p.bc[1] == BC_COPY && p.bc[2] == BC_COPY) {
+        if (p.phase_axes == PH_Z) {
+            if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, false, PH_Z, false, true>(p, m, grid, first, s);
+            return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_Z, false, true>(p, m, grid, first, s);
+        }
+        if (p.phase_axes == PH_NONE) {
+            if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, false, PH_NONE, false, true>(p, m, grid, first, s);
+            return launch_tma_t<SCHEME_KSPACE, false, false, TWV, false, PH_NONE, false, true>(p, m, grid, first, s);
+        }
     }
     if (vel) return launch_tma_t<SCHEME_KSPACE, true, false, TWV, true, PH_ALL, false, true>(p, m, grid, first, s);
     return launch_tma_t<SCHEME_KSPACE, false, false, TWV, true, PH_ALL, false, true>(p, m, grid, first, s);

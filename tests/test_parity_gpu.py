@@ -193,14 +193,15 @@ def test_several_pulses_in_one_step(scheme, btlib, oracle_lib):
             assert rel_err(st, ref) <= F32_MT_TOL
 
 
-@pytest.mark.parametrize("scheme", [0, 1])
-def test_pulse_steps_on_the_fast_path(scheme, btlib, monkeypatch):
+@pytest.mark.parametrize("scheme,grad", [(0, True), (1, True), (1, False)])
+def test_pulse_steps_on_the_fast_path(scheme, grad, btlib, monkeypatch):
     """FP32 steps whose pulses are all fixed-angle run on the fast path (the
     step's rotation applied before its sums, the run of fast steps going on:
     with a pulse in every 32-step window, n steps take n launches and one
     closing launch) and give the generic kernel's fields and M(t) within
     1e-5: a multi-echo train (a 90 at step 0, then a 180 every 8 steps) with
-    flow; KSPACE with a gradient along z, REFERENCE with the cross product."""
+    flow; KSPACE with a gradient along z and without one, REFERENCE with the
+    cross product."""
     import initializator_gb300 as bt
     from initializator_gb300 import geometry
     shape = (40, 24, 48)
@@ -214,7 +215,8 @@ def test_pulse_steps_on_the_fast_path(scheme, btlib, monkeypatch):
     sched = {}
     if scheme == bt.BT_SCHEME_KSPACE:
         kw.update(gamma=bt.GAMMA_PROTON)
-        sched = dict(grad_wave=bt.kspace_waveform_pgse(n, dt, 0.1, 6 * dt, 30 * dt, axis=(0.0, 0.0, 1.0)))
+        if grad:
+            sched = dict(grad_wave=bt.kspace_waveform_pgse(n, dt, 0.1, 6 * dt, 30 * dt, axis=(0.0, 0.0, 1.0)))
     else:
         kw.update(main_field=(0.2, 0.3, 0.9), grad=(0.02, -0.03, 0.05), vector_mult=1)
     st0 = np.zeros((3,) + shape)
