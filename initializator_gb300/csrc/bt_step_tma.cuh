@@ -1,11 +1,14 @@
 // FP32 fast path of the fused step (K1, TMA form) for sm_103a.
 //
-// Same update and M(t) as step_kernel (bt_step.cuh), for steps without pulses:
+// Same update and M(t) as step_kernel (bt_step.cuh), for steps without pulses
+// and steps whose pulses are all fixed-angle (the RF instances apply the
+// step's product rotation to each voxel's lab-frame value before the sums):
 //   * a CTA owns a 128 x 8 column tile (64 x 16 for grids a 128-wide tile
-//     would pad more: see Tile) and marches through a z-chunk (the
-//     column split into P.zsplit even chunks; odd chunks march downwards, so
-//     the plane two neighbouring chunks share is read by both at about the
-//     same moment and the second read hits L2);
+//     would pad more: see Tile) and marches through a z-chunk (the first
+//     P.zlong columns split into P.zsplit even chunks, the others into one
+//     fewer; odd chunks march downwards, so the plane two neighbouring chunks
+//     share is read by both at about the same moment and the second read hits
+//     L2);
 //   * each z-plane of the tile (the three field components with a one-voxel
 //     x/y halo, upwind cell velocities, geometry code) is fetched by one thread with
 //     cp.async.bulk.tensor into a 3-slot shared-memory ring, completion
