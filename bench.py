@@ -367,6 +367,18 @@ CPMG_ECHO = 10               # steps between the multi-echo leg's refocusing pul
 CPMG_G = 0.05                # T/m, its constant gradient along z
 
 
+def cpmg_schedule(n):
+    """The multi-echo leg's schedule over n steps: a constant gradient
+    CPMG_G along z (with 16 spare steps), a 90-degree pulse about y at step 0
+    and a 180-degree pulse about x at CPMG_ECHO / 2 and every CPMG_ECHO steps
+    after it."""
+    wave = np.zeros((n + 16, 3))
+    wave[:, 2] = CPMG_G
+    rf = [(0, 2, 0.5 * math.pi, (0.0, 1.0, 0.0))]
+    rf += [(q, 2, math.pi, (1.0, 0.0, 0.0)) for q in range(CPMG_ECHO // 2, n, CPMG_ECHO)]
+    return wave, rf
+
+
 def run_cpmg(s, stream, st0, nvox, value_plain):
     """Multi-echo (CPMG) train on the C2 handle (same geometry, flow and
     z-chunking): a 90-degree pulse about y at step 0, then a 180-degree pulse
@@ -378,11 +390,7 @@ def run_cpmg(s, stream, st0, nvox, value_plain):
     step is its own launch (no CUDA graph)."""
     import torch
     S = STEPS_PER_ITER
-    n = 3 * S
-    wave = np.zeros((n + 16, 3))
-    wave[:, 2] = CPMG_G
-    rf = [(0, 2, 0.5 * math.pi, (0.0, 1.0, 0.0))]
-    rf += [(q, 2, math.pi, (1.0, 0.0, 0.0)) for q in range(CPMG_ECHO // 2, n, CPMG_ECHO)]
+    wave, rf = cpmg_schedule(3 * S)
     s.set_step(0)
     s.set_schedule(rf, grad_wave=wave)
     s.set_state(st0)
